@@ -1,0 +1,332 @@
+#!/usr/bin/env python3
+"""Benchmark of the ray-query hot path on one GB300.
+
+Workload (a "step"): config 3 -- closest-hit traversal of 16,777,216
+incoherent rays (origins uniform in the unit cube, directions uniform on the
+sphere, tmin 1e-4, tmax inf) through a 4,194,304-triangle soup (centroids
+uniform in the cube, vertex offsets N(0, 0.002^2)), BVH built on the host in
+the reference node layout (sorted leaves).  Synthetic, seeded inputs.
+
+value  : rays/s with rays and hits resident in HBM (one rt_trace per step)
+e2e    : the same through rt_trace_host with pinned host buffers, so every
+         step includes the 512 MiB ray upload and 128 MiB hit download
+roofline: algorithmic bytes per ray (32 ray + 8 hit + 32 per node box tested
+         + 48 per triangle tested, counts of the canonical traversal) times
+         rays per launch over the kernel's event-timed launch duration,
+         against the measured HBM copy bandwidth
+cpu_baseline: the CPU oracle's restatement of the reference traversal
+         (raytraceBVH.comp:195-265, push-left/go-right, no culling) on a
+         bounded sample of the same rays, all host threads
+
+--impl reference runs that CPU restatement alone as the reference arm.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "closest-hit Grays/s batched vs plain per-call launch; served p50/p99 latency"
+UNIT = "Grays/s"
+N_TRIS = 4_194_304
+N_RAYS = 16_777_216
+SEED = 3
+CPU_SAMPLE = 262_144
+COUNT_SAMPLE = 65_536
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=20)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    p.add_argument("--tris", type=int, default=N_TRIS)
+    p.add_argument("--rays", type=int, default=N_RAYS)
+    p.add_argument("--leaf-size", type=int, default=0)
+    p.add_argument("--cpu-sample", type=int, default=CPU_SAMPLE)
+    p.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    p.add_argument("--no-e2e", action="store_true")
+    return p.parse_args()
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons, sampled every 200 ms."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.rows = []
+        self.proc = None
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) >= 8:
+                self.rows.append((time.time(), parts))
+
+    def stop(self):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self, t0: float, t1: float) -> dict:
+        rows = [r for (t, r) in self.rows if t0 <= t <= t1] or [r for (_, r) in self.rows]
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+
+        def num(x):
+            try:
+                return float(x)
+            except ValueError:
+                return None
+
+        sm = [num(r[0]) for r in rows if num(r[0]) is not None]
+        mx = [num(r[1]) for r in rows if num(r[1]) is not None]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[4 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows),
+                "power_w_max": max((num(r[2]) or 0.0) for r in rows)}
+
+
+def measured_peak():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        try:
+            return float(json.loads(p.read_text())["hbm_gbs"]), "measured"
+        except (KeyError, ValueError):
+            pass
+    return 6800.0, "fallback"
+
+
+def workload(n_tris: int, n_rays: int):
+    import raytracergpu_mastersproject_gb300 as rt
+
+    tris = rt.gen_soup(SEED, 0, n_tris, 1.0, 0.002)
+    rays = rt.gen_rays(SEED, 0, n_rays, 1.0, 1e-4, float("inf"))
+    return tris, rays
+
+
+def cpu_leg(tris, nodes, rays, sample: int) -> tuple[dict, dict]:
+    """CPU baseline: the oracle's reference-order traversal on `sample` rays
+    with every host thread; plus canonical traversal counts (work per ray)."""
+    from oracle import oracle as orc
+
+    orc.build()
+    S = orc.Scene(tris, nodes)
+    cores = os.cpu_count() or 1
+    sub = np.ascontiguousarray(rays[:sample])
+    t0 = time.perf_counter()
+    ref_hits, st = orc.trace(S, sub, canonical=False, nthreads=cores)
+    dt = time.perf_counter() - t0
+    cnt = np.ascontiguousarray(rays[:COUNT_SAMPLE])
+    can_hits, cst = orc.trace(S, cnt, canonical=True, nthreads=cores)
+    counts = {"node_boxes_per_ray": float(cst[0]) / len(cnt), "tri_tests_per_ray": float(cst[1]) / len(cnt),
+              "sample": len(cnt)}
+    base = {"value": len(sub) / dt / 1e9, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": f"first {len(sub)} rays of the config-3 batch, oracle restatement of hitBVH "
+                      f"(reference order, no culling, sorted-leaf BVH), {cores} threads, {dt:.2f} s"}
+    return base, {"counts": counts, "ref_hits": ref_hits, "can_hits": can_hits}
+
+
+def run_reference(args):
+    """Reference arm: the CPU restatement of the reference traversal, timed."""
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return
+    import raytracergpu_mastersproject_gb300 as rt
+    from oracle import oracle as orc
+
+    tris, rays = workload(args.tris, args.rays)
+    nodes = rt.build_bvh(tris)
+    orc.build()
+    S = orc.Scene(tris, nodes)
+    cores = os.cpu_count() or 1
+    per = max(1024, min(args.cpu_sample, 65_536))
+    off = 0
+    for _ in range(args.warmup):
+        orc.trace(S, rays[off:off + per], nthreads=cores)
+        off = (off + per) % (len(rays) - per)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        orc.trace(S, rays[off:off + per], nthreads=cores)
+        off = (off + per) % (len(rays) - per)
+    dt = time.perf_counter() - t0
+    v = per * args.steps / dt / 1e9
+    line = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "impl": "reference",
+            "config": {"workload": f"config 3: {args.tris}-triangle soup, incoherent rays, closest-hit; "
+                                   f"each step traces a bounded sample of {per} rays on the host cores",
+                       "triangles": args.tris, "rays_per_step": per},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
+                             "sample": f"{per} rays per step, oracle restatement of hitBVH (reference order, "
+                                       f"no culling, sorted-leaf BVH); the reference itself is Vulkan/GLSL and "
+                                       f"cannot run here"},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    import torch
+
+    import raytracergpu_mastersproject_gb300 as rt
+
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    dist = None
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    tris, rays = workload(args.tris, args.rays)
+    scene = rt.Scene(tris, leaf_size=args.leaf_size)
+    info = scene.info()
+    n = len(rays)
+    d_rays = torch.from_numpy(rays.view(np.uint8)).cuda()
+    d_hits = torch.empty(n * 8, dtype=torch.uint8, device="cuda")
+    stream = torch.cuda.current_stream()
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+
+    for _ in range(args.warmup):
+        scene.trace(d_rays, d_hits)
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.5)
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    barrier()
+    torch.cuda.synchronize()
+    t_start = time.time()
+    g0 = torch.cuda.Event(enable_timing=True)
+    g1 = torch.cuda.Event(enable_timing=True)
+    g0.record(stream)
+    for s in range(args.steps):
+        evs[s][0].record(stream)
+        scene.trace(d_rays, d_hits, stream=stream)
+        evs[s][1].record(stream)
+    g1.record(stream)
+    torch.cuda.synchronize()
+    barrier()
+    t_end = time.time()
+    total_ms = g0.elapsed_time(g1)
+    launch_ms = [a.elapsed_time(b) for a, b in evs]
+    if dist is not None:
+        t = torch.tensor([total_ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    ms_step = total_ms / args.steps
+    value = n * ws / (ms_step / 1e3) / 1e9
+
+    e2e = None
+    if not args.no_e2e:
+        h_rays = torch.from_numpy(rays.view(np.uint8)).pin_memory()
+        h_hits = torch.empty(n * 8, dtype=torch.uint8).pin_memory()
+        hr = h_rays.numpy().view(rt.RAY_DTYPE)
+        hh = h_hits.numpy().view(rt.HIT_DTYPE)
+        scene.trace_host(hr, out=hh)
+        k = max(3, min(args.steps, 10))
+        barrier()
+        t0 = time.perf_counter()
+        for _ in range(k):
+            scene.trace_host(hr, out=hh)
+        dt = time.perf_counter() - t0
+        barrier()
+        e2e = {"value": n * ws / (dt / k) / 1e9, "unit": UNIT, "h2d_bytes_per_step": n * 32,
+               "d2h_bytes_per_step": n * 8, "steps": k, "ms_per_step": dt / k * 1e3,
+               "path": "rt_trace_host, pinned host buffers, copies overlapped with tracing in 2 Mi-ray chunks"}
+        hits_dev = d_hits.cpu().numpy().view(rt.HIT_DTYPE)
+        assert np.array_equal(hits_dev.view(np.uint64), hh.view(np.uint64)), "e2e hits differ from device hits"
+    clocks.stop()
+    clk = clocks.summary(t_start, t_end)
+
+    if rank != 0:
+        return
+    peak, peak_kind = measured_peak()
+    cpu_base, counts, parity = None, None, None
+    if not args.no_cpu:
+        nodes = scene.nodes()
+        cpu_base, extra = cpu_leg(tris, nodes, rays, min(args.cpu_sample, n))
+        counts = extra["counts"]
+        got = d_hits.cpu().numpy().view(rt.HIT_DTYPE)
+        k = len(extra["ref_hits"])
+        parity = {"rays_checked": k, "id_mismatches_vs_reference_order": int((got["prim"][:k] != extra["ref_hits"]["prim"]).sum())}
+    roof = None
+    if counts:
+        b_ray = 32 + 8 + 32 * counts["node_boxes_per_ray"] + 48 * counts["tri_tests_per_ray"]
+        avg_launch = statistics.mean(launch_ms) / 1e3
+        achieved = b_ray * n / avg_launch / 1e9
+        roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "traffic": None, "peak_kind": peak_kind,
+                "bytes_per_ray": b_ray, "node_boxes_per_ray": counts["node_boxes_per_ray"],
+                "tri_tests_per_ray": counts["tri_tests_per_ray"],
+                "kernel": "k_trace<closest> (persistent warps, BVH2 child-box nodes)",
+                "avg_launch_ms": avg_launch * 1e3}
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "config 3: 4,194,304-triangle soup, 16,777,216 incoherent rays, closest-hit"
+                       if (args.tris, args.rays) == (N_TRIS, N_RAYS) else
+                       f"config-3 shape: {args.tris} triangles, {args.rays} rays, closest-hit",
+                       "triangles": args.tris, "rays": n, "bvh": "host LBVH, sorted leaves",
+                       "leaf_size": info.leaf_size, "device_nodes": info.device_nodes, "bvh_depth": info.depth,
+                       "l2": "inputs larger than L2 (rays 512 MiB, nodes+triangles 512 MiB); no flush",
+                       "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU"},
+            "roofline": roof, "cpu_baseline": cpu_base, "e2e": e2e, "clocks": clk,
+            "gpu_launches": args.steps, "parity_sample": parity,
+            "scene_build_s": info.build_seconds}
+    print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

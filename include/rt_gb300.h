@@ -1,0 +1,256 @@
+/*
+ * rt_gb300.h -- C ABI of the GB300 (sm_103a) ray-tracing hot path.
+ *
+ * This header is the drop-in boundary for the raytrace compute pass of
+ * RaytracerGPU_MastersProject (Vulkan).  In the reference, C++ host code fills a
+ * descriptor set (RaytracerBVH.cpp:202-238, 677-685):
+ *
+ *   b0 ParameterUBO       camera, counts, depth, randomState   (raytraceBVH.comp:7-18)
+ *   b1 storage image      RGBA32F accumulator, RNG carry in a   (raytraceBVH.comp:22, 349-374)
+ *   b2 Triangle SSBO      64-byte records                      (definitions.glsl:15-21)
+ *   b3 Sphere SSBO        32-byte records                      (definitions.glsl:23-28)
+ *   b4 Material SSBO      32-byte records                      (definitions.glsl:10-13)
+ *   b5 HLBVHNode SSBO     40-byte nodes, 2N-1 of them           (definitions.glsl:66-72)
+ *
+ * and records vkCmdDispatch((W/32)+1, (H/32)+1, 1) once per ray per pixel
+ * (RaytracerBVH.cpp:1025-1050).  Here the same buffers are handed to
+ * rt_scene_create / rt_render, and the dispatch becomes one stream-ordered call.
+ * The BVH is built on the host in the reference node layout when no node
+ * buffer is supplied.
+ *
+ * Conventions
+ *   - Every entry point returns rt_status; nothing throws across the ABI.
+ *     rt_last_error_string() describes the last failure of the calling thread.
+ *   - "stream" is a cudaStream_t passed as void* (NULL = legacy default stream).
+ *   - Pointers named d_* are device pointers; h_* are host pointers.
+ *   - Scenes are immutable after creation; tracing one scene from several
+ *     streams at once is safe.
+ */
+#ifndef RT_GB300_H
+#define RT_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define RT_ABI_VERSION 1u
+
+/* ---------------------------------------------------------------- status */
+typedef enum rt_status {
+  RT_OK = 0,
+  RT_EINVAL = 1,      /* bad argument (null pointer, size, index out of range) */
+  RT_ENOMEM = 2,      /* device or host allocation failed / over budget       */
+  RT_ETIMEOUT = 3,    /* bounded host wait ran out                            */
+  RT_ESTACK = 4,      /* BVH deeper than the traversal stack                  */
+  RT_ECUDA = 5,       /* CUDA runtime error                                   */
+  RT_EBUSY = 6,       /* admission refused for now (serving)                  */
+  RT_ECANCELED = 7,   /* request cancelled                                    */
+  RT_ENOTFOUND = 8,   /* unknown scene / request id                           */
+  RT_EUNSUPPORTED = 9 /* option not supported by this build                   */
+} rt_status;
+
+/* ------------------------------------------------ enums of the reference */
+/* Material types: definitions.glsl:79-82, SceneTypes.hpp:14-19. */
+enum { RT_MAT_LIGHT = 0, RT_MAT_DIFFUSE = 1, RT_MAT_METALLIC = 2, RT_MAT_DIELECTRIC = 3 };
+/* Primitive types: definitions.glsl:84-85. */
+enum { RT_PRIM_SPHERE = 0, RT_PRIM_TRIANGLE = 1 };
+
+/* ------------------------------------------------- records (std430 size) */
+/* Triangle, 64 B: vec4 v0,v1,v2 (w unused), materialIndex@48, modelIndex@52.
+ * definitions.glsl:15-21, SceneTypes.hpp:41-47. */
+typedef struct RtTriangle64 {
+  float v0[4];
+  float v1[4];
+  float v2[4];
+  uint32_t materialIndex;
+  uint32_t modelIndex;
+  uint32_t _pad[2];
+} RtTriangle64;
+
+/* Sphere, 32 B: vec4 center, radius@16, materialIndex@20, modelIndex@24.
+ * definitions.glsl:23-28, SceneTypes.hpp:62-66. */
+typedef struct RtSphere32 {
+  float center[4];
+  float radius;
+  uint32_t materialIndex;
+  uint32_t modelIndex;
+  uint32_t _pad;
+} RtSphere32;
+
+/* Material, 32 B: vec4 albedo, materialType@16 (definitions.glsl:10-13,
+ * SceneTypes.hpp:82-84).  fuzz@20 and ior@24 sit in the record's std430 tail
+ * padding; the reference never reads them.  Only RT_SHADE_EXTENDED uses them. */
+typedef struct RtMaterial32 {
+  float albedo[4];
+  uint32_t materialType;
+  float fuzz;
+  float ior;
+  uint32_t _pad;
+} RtMaterial32;
+
+/* Model matrix, 64 B, column-major mat4 (definitions.glsl:6-8, SceneTypes.hpp:32-33). */
+typedef struct RtModel64 {
+  float m[16];
+} RtModel64;
+
+/* BVH node, 40 B (definitions.glsl:52-56,66-72; SceneTypes.hpp:107-123).
+ * Leaf <=> left == 0 && right == 0 (raytraceBVH.comp:213).  Node 0 is the root. */
+typedef struct RtBVHNode40 {
+  float minX, maxX, minY, maxY, minZ, maxZ;
+  uint32_t left;
+  uint32_t right;
+  uint32_t primitiveIndex;
+  uint32_t primitiveType;
+} RtBVHNode40;
+
+/* ParameterUBO, std140 (raytraceBVH.comp:7-18; RaytracerBVH.hpp:31-42):
+ * camPos@0 camLookAt@16 camUpDir@32 verticalFOV@48 numTriangles@52
+ * numSpheres@56 numMaterials@60 numLights@64 maxRayTraceDepth@68
+ * randomState@72; padded to 80 B like the C++ struct. */
+typedef struct RtRaytraceUBO {
+  float camPos[4];
+  float camLookAt[4];
+  float camUpDir[4];
+  float verticalFOV;
+  uint32_t numTriangles;
+  uint32_t numSpheres;
+  uint32_t numMaterials;
+  uint32_t numLights;
+  uint32_t maxRayTraceDepth;
+  uint32_t randomState;
+  uint32_t _pad;
+} RtRaytraceUBO;
+
+/* A ray query, 32 B: origin, tmin, direction, tmax.  Struct Ray of
+ * definitions.glsl:35-38 plus the interval that sceneHit fixes at
+ * [0.001, 1e7] (raytraceBVH.comp:267-274). */
+typedef struct RtRay {
+  float org[3];
+  float tmin;
+  float dir[3];
+  float tmax;
+} RtRay;
+
+/* A hit, 8 B.  prim = triangle index, or (sphere index | RT_HIT_SPHERE_BIT),
+ * or RT_NO_HIT; t = ray parameter of the hit (+inf on a miss). */
+typedef struct RtHit {
+  uint32_t prim;
+  float t;
+} RtHit;
+
+#define RT_NO_HIT 0xFFFFFFFFu
+#define RT_HIT_SPHERE_BIT 0x80000000u
+
+/* ------------------------------------------------------------------ scene */
+typedef struct rt_scene rt_scene;
+
+enum {
+  RT_BVH_SORTED = 0,    /* leaf k holds the k-th Morton-sorted primitive (default) */
+  RT_BVH_REFERENCE = 1  /* leaf k holds primitive k, as ConstructHLBVH.comp:152-169 */
+};
+
+typedef struct RtSceneDesc {
+  const RtTriangle64* triangles;  /* host, num_triangles records */
+  uint32_t num_triangles;
+  const RtSphere32* spheres;      /* host, may be NULL if num_spheres == 0 */
+  uint32_t num_spheres;
+  const RtMaterial32* materials;  /* host, may be NULL if num_materials == 0 */
+  uint32_t num_materials;
+  const RtModel64* models;        /* host; NULL = vertices are already in world space */
+  uint32_t num_models;
+  const RtBVHNode40* nodes;       /* host; NULL = build on the host (bvh_mode) */
+  uint32_t num_nodes;             /* 2*(num_triangles+num_spheres)-1 when nodes != NULL */
+  uint32_t bvh_mode;              /* RT_BVH_SORTED | RT_BVH_REFERENCE */
+  uint32_t leaf_size;             /* max triangles per device leaf after collapsing; 0 = default */
+} RtSceneDesc;
+
+typedef struct RtSceneInfo {
+  uint32_t num_triangles;
+  uint32_t num_spheres;
+  uint32_t num_materials;
+  uint32_t num_nodes;          /* reference-layout node count, 2N-1 */
+  uint32_t device_nodes;       /* internal nodes of the device BVH */
+  uint32_t depth;              /* longest root-to-leaf path of the device BVH */
+  uint32_t leaf_size;
+  uint32_t bvh_mode;
+  uint64_t device_bytes;       /* device memory held by the scene */
+  double build_seconds;        /* host BVH build + conversion time */
+} RtSceneInfo;
+
+/* Replaces the scene upload + S1 BVH build of the reference
+ * (RaytraceScene.cpp:157-248, RaytracerBVH.cpp:479-550, 734-997).
+ * Copies the host arrays, builds the BVH on the host when nodes == NULL,
+ * and uploads the device form.  The caller keeps ownership of its arrays. */
+rt_status rt_scene_create(const RtTriangle64* triangles, uint32_t num_triangles,
+                          const RtSphere32* spheres, uint32_t num_spheres,
+                          const RtMaterial32* materials, uint32_t num_materials,
+                          const RtBVHNode40* nodes, rt_scene** out_scene);
+rt_status rt_scene_create_ex(const RtSceneDesc* desc, rt_scene** out_scene);
+rt_status rt_scene_destroy(rt_scene* scene);
+rt_status rt_scene_get_info(const rt_scene* scene, RtSceneInfo* out_info);
+/* Copies the reference-layout node array (2N-1 records) the scene was built
+ * from, i.e. the content of the HLBVHNode SSBO (RaytracerBVH.cpp:536-542). */
+rt_status rt_scene_get_nodes(const rt_scene* scene, RtBVHNode40* h_out, uint32_t capacity);
+
+/* Host BVH build alone (no device work): the six S1 passes of
+ * RaytracerBVH.cpp:778-991 in the reference node layout.  out_nodes holds
+ * 2*(num_triangles+num_spheres)-1 records.  models may be NULL. */
+rt_status rt_build_bvh(const RtTriangle64* triangles, uint32_t num_triangles,
+                       const RtSphere32* spheres, uint32_t num_spheres,
+                       const RtModel64* models, uint32_t num_models,
+                       uint32_t bvh_mode, RtBVHNode40* out_nodes);
+
+/* ------------------------------------------------------------------ trace */
+enum {
+  RT_TRACE_CLOSEST = 0,  /* closest hit in [tmin, tmax] (hitBVH, raytraceBVH.comp:195-265) */
+  RT_TRACE_ANY = 1       /* any hit in [tmin, tmax] (occlusion) */
+};
+
+/* Traces n rays resident on the device; writes n hits.  Stream-ordered. */
+rt_status rt_trace(rt_scene* scene, const RtRay* d_rays, uint32_t n, RtHit* d_hits,
+                   uint32_t flags, void* stream);
+/* Same with host buffers (pinned or pageable): the library stages the rays
+ * through the device in chunks, overlapping copies with tracing, and returns
+ * when h_hits is filled. */
+rt_status rt_trace_host(rt_scene* scene, const RtRay* h_rays, uint32_t n, RtHit* h_hits,
+                        uint32_t flags, void* stream);
+
+/* ----------------------------------------------------------------- render */
+enum {
+  RT_SHADE_REFERENCE = 0, /* LIGHT emits, DIFFUSE scatters, others terminate, background 0 */
+  RT_SHADE_EXTENDED = 1   /* + metal (fuzz), dielectric (ior), background colour */
+};
+
+typedef struct RtRenderOptions {
+  uint32_t shade_mode;     /* RT_SHADE_REFERENCE | RT_SHADE_EXTENDED */
+  float background[3];     /* used by RT_SHADE_EXTENDED only */
+} RtRenderOptions;
+
+/* The S2 pass (RaytracerBVH.cpp:998-1078): spp samples per pixel of
+ * raytraceBVH.comp:main, each adding its colour to d_accum (W*H float4,
+ * row-major, pixel (x,y) at index y*W+x) and leaving the RNG carry in alpha,
+ * exactly as spp back-to-back dispatches would.  opt may be NULL (reference). */
+rt_status rt_render(rt_scene* scene, const RtRaytraceUBO* ubo, float* d_accum,
+                    uint32_t width, uint32_t height, uint32_t spp,
+                    const RtRenderOptions* opt, void* stream);
+/* The per-frame clear of the accumulator to (0,0,0,1) (RaytracerBVH.cpp:772-776). */
+rt_status rt_accum_clear(float* d_accum, uint32_t width, uint32_t height, void* stream);
+/* The present pass's colour math, clamp(sqrt(sum/spp), 0, 1)
+ * (SingleTriangleFullScreen.frag:13-18), into a W*H float4 device buffer. */
+rt_status rt_resolve(const float* d_accum, uint32_t width, uint32_t height, uint32_t spp,
+                     float* d_out, void* stream);
+
+/* --------------------------------------------------------------- utility */
+const char* rt_last_error_string(void);
+uint32_t rt_abi_version(void);
+/* Waits for the stream with a deadline; RT_ETIMEOUT when it runs out. */
+rt_status rt_stream_wait(void* stream, double timeout_seconds);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* RT_GB300_H */

@@ -1,0 +1,965 @@
+/*
+ * rt_oracle.c -- CPU restatement of the reference ray-tracing hot path.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This file is the checker: tests/, the smoke entry
+ * point and bench.py's CPU-baseline leg load it.  The product (the CUDA library
+ * under raytracergpu_mastersproject_gb300/) never links or calls it.
+ *
+ * What it restates (paths relative to the RaytracerGPU_MastersProject source):
+ *   shaders/compute/raytraceBVH.comp:50-375   camera, triangleHit, sphereHit,
+ *                                              AABBhitCheck, hitBVH, rayColor,
+ *                                              emitted, scatter, main
+ *   shaders/include/random.glsl:10-62          PCG-hash RNG and samplers
+ *   shaders/include/definitions.glsl:6-85      record layouts and enums
+ *   shaders/compute/ModelSpaceToWorldSpace.comp:32-48,
+ *   GetEnclosingAABB.comp:40-109, GenerateMortonCodesOfPrimitives.comp:38-93,
+ *   RadixSortSimple.comp:52-157, ConstructHLBVH.comp:41-214,
+ *   ConstructAABBsOfInternalNodes.comp:27-64  the six BVH-build passes
+ *   shaders/fragment/SingleTriangleFullScreen.frag:13-18   resolve
+ *
+ * Parity unpinned: the reference ships no tests, fixtures or golden vectors,
+ * and it cannot run here (GLSL compute shaders behind Vulkan, no graphics
+ * stack).  This file is pinned only by being a line-by-line restatement, by
+ * a published worked example (Karras 2012, Fig. 3) for the tree builder, and
+ * by its own committed fixtures.
+ *
+ * Arithmetic contract (shared with the CUDA kernels; built with
+ * -ffp-contract=off, no fast-math): every + - * / sqrt is one IEEE-754
+ * binary32 operation, evaluated left to right as written in the GLSL;
+ *   dot(a,b)    = (a.x*b.x + a.y*b.y) + a.z*b.z
+ *   cross(a,b)  = (a.y*b.z - a.z*b.y, a.z*b.x - a.x*b.z, a.x*b.y - a.y*b.x)
+ *   normalize(v)= v / sqrt(dot(v,v))        (component-wise division)
+ *   min/max     = fminf/fmaxf (a NaN operand yields the other operand)
+ *   uint(f)     = saturating float->uint (NaN and negatives -> 0)
+ *   sin/cos     = rt_sin/rt_cos below (Cody-Waite reduction + Taylor
+ *                 polynomials), so that host and device agree bit for bit.
+ * Defined where the reference is undefined or degenerate:
+ *   - GetEnclosingAABB.comp:69-70 reads uninitialised localMin/localMax;
+ *     here the fold starts from the SSBO's preset +-1e9 only.
+ *   - triangleHit on a zero-area triangle yields t = NaN, which the reference
+ *     accepts as a hit; here a NaN t is rejected.
+ *   - the reference's 128-entry stack is never checked; here overflow sets
+ *     a status bit and ends the ray.
+ */
+#include <math.h>
+#include <pthread.h>
+#include <stdatomic.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+
+/* ------------------------------------------------------------ records -- */
+/* definitions.glsl:15-21 */
+typedef struct { float v0[4], v1[4], v2[4]; uint32_t mat, model, pad[2]; } OTri;
+/* definitions.glsl:23-28 */
+typedef struct { float c[4]; float r; uint32_t mat, model, pad; } OSph;
+/* definitions.glsl:10-13 (+ fuzz, ior in the std430 tail padding) */
+typedef struct { float albedo[4]; uint32_t type; float fuzz, ior; uint32_t pad; } OMat;
+/* definitions.glsl:52-56,66-72 */
+typedef struct { float minX, maxX, minY, maxY, minZ, maxZ; uint32_t left, right, prim, ptype; } ONode;
+/* raytraceBVH.comp:7-18 */
+typedef struct {
+  float camPos[4], camLookAt[4], camUpDir[4];
+  float fov;
+  uint32_t nT, nS, nM, nL, depth, randomState, pad;
+} OUbo;
+typedef struct { float o[3]; float tmin; float d[3]; float tmax; } ORay;
+typedef struct { uint32_t prim; float t; } OHit;
+
+_Static_assert(sizeof(OTri) == 64, "Triangle is 64 B");
+_Static_assert(sizeof(OSph) == 32, "Sphere is 32 B");
+_Static_assert(sizeof(OMat) == 32, "Material is 32 B");
+_Static_assert(sizeof(ONode) == 40, "HLBVHNode is 40 B");
+_Static_assert(sizeof(OUbo) == 80, "ParameterUBO is 80 B");
+_Static_assert(sizeof(ORay) == 32, "ray is 32 B");
+
+typedef struct {
+  const OTri* tris; uint32_t nt;
+  const OSph* sph; uint32_t ns;
+  const OMat* mats; uint32_t nm;
+  const ONode* nodes; uint32_t nn;
+} OScene;
+
+#define LIGHT_MATERIAL 0u      /* definitions.glsl:79-82 */
+#define DIFFUSE_MATERIAL 1u
+#define METALLIC_MATERIAL 2u
+#define DIELECTRIC_MATERIAL 3u
+#define SPHERE_PRIMITIVE 0u    /* definitions.glsl:84-85 */
+#define TRIANGLE_PRIMITIVE 1u
+#define NO_HIT 0xFFFFFFFFu
+#define SPHERE_BIT 0x80000000u
+
+/* ------------------------------------------------------------- vec3 ---- */
+typedef struct { float x, y, z; } v3;
+static inline v3 V(float x, float y, float z) { v3 r = {x, y, z}; return r; }
+static inline v3 vadd(v3 a, v3 b) { return V(a.x + b.x, a.y + b.y, a.z + b.z); }
+static inline v3 vsub(v3 a, v3 b) { return V(a.x - b.x, a.y - b.y, a.z - b.z); }
+static inline v3 vmul(v3 a, v3 b) { return V(a.x * b.x, a.y * b.y, a.z * b.z); }
+static inline v3 vscale(v3 a, float s) { return V(a.x * s, a.y * s, a.z * s); }
+static inline v3 vdivs(v3 a, float s) { return V(a.x / s, a.y / s, a.z / s); }
+static inline v3 vneg(v3 a) { return V(-a.x, -a.y, -a.z); }
+static inline float vdot(v3 a, v3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+static inline v3 vcross(v3 a, v3 b) {
+  return V(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
+}
+static inline v3 vnormalize(v3 a) { return vdivs(a, sqrtf(vdot(a, a))); }
+static inline v3 V4(const float* p) { return V(p[0], p[1], p[2]); }
+
+static inline uint32_t f2u_sat(float f) {
+  if (!(f > 0.0f)) return 0u;
+  if (f >= 4294967296.0f) return 0xFFFFFFFFu;
+  return (uint32_t)f;
+}
+
+/* ---------------------------------------------------------- sin / cos -- */
+/* Cody-Waite reduction by pi/2 in three binary32 parts, then Taylor
+ * polynomials (degree 9 / 10) on [-pi/4, pi/4].  Coefficients are the
+ * binary32 roundings of +-1/n!.  Identical operation order in the device code. */
+static const float RT_2_OVER_PI = 0x1.45f306p-1f;
+static const float RT_PIO2_1 = 0x1.92p+0f;
+static const float RT_PIO2_2 = 0x1.fb6p-12f;
+static const float RT_PIO2_3 = -0x1.777a5cp-25f;
+static const float RT_S1 = -0x1.555556p-3f, RT_S2 = 0x1.111112p-7f, RT_S3 = -0x1.a01a02p-13f,
+                   RT_S4 = 0x1.71de3ap-19f;
+static const float RT_C1 = -0x1p-1f, RT_C2 = 0x1.555556p-5f, RT_C3 = -0x1.6c16c2p-10f,
+                   RT_C4 = 0x1.a01a02p-16f, RT_C5 = -0x1.27e4fcp-22f;
+
+static void rt_sincos(float x, float* s_out, float* c_out) {
+  float kf = rintf(x * RT_2_OVER_PI);
+  int k = (int)kf;
+  float r = x - kf * RT_PIO2_1;
+  r = r - kf * RT_PIO2_2;
+  r = r - kf * RT_PIO2_3;
+  float r2 = r * r;
+  float ps = RT_S4;
+  ps = ps * r2 + RT_S3;
+  ps = ps * r2 + RT_S2;
+  ps = ps * r2 + RT_S1;
+  float s = r + r * (r2 * ps);
+  float pc = RT_C5;
+  pc = pc * r2 + RT_C4;
+  pc = pc * r2 + RT_C3;
+  pc = pc * r2 + RT_C2;
+  pc = pc * r2 + RT_C1;
+  float c = 1.0f + r2 * pc;
+  switch (k & 3) {
+    case 0: *s_out = s; *c_out = c; break;
+    case 1: *s_out = c; *c_out = -s; break;
+    case 2: *s_out = -s; *c_out = -c; break;
+    default: *s_out = -c; *c_out = s; break;
+  }
+}
+float orc_sin(float x) { float s, c; rt_sincos(x, &s, &c); return s; }
+float orc_cos(float x) { float s, c; rt_sincos(x, &s, &c); return c; }
+
+/* --------------------------------------------------------------- RNG --- */
+static const float ORC_PI = 0x1.921fb6p+1f; /* random.glsl:7, 3.1415926535897932385 as float */
+
+/* random.glsl:12-14 */
+uint32_t orc_step_rng(uint32_t s) { return s * 747796405u + 1u; }
+/* random.glsl:17-22 */
+static inline float step_and_output(uint32_t* s) {
+  *s = orc_step_rng(*s);
+  uint32_t word = ((*s >> ((*s >> 28u) + 4u)) ^ *s) * 277803737u;
+  word = (word >> 22u) ^ word;
+  return (float)word / 4294967295.0f;
+}
+/* random.glsl:9: per-invocation seed */
+uint32_t orc_seed(uint32_t x, uint32_t y, uint32_t randomState) {
+  return (600u * x + y) * (randomState + 1u);
+}
+/* random.glsl:28-30 */
+static inline float random_range(uint32_t* s, float mn, float mx) {
+  return mn + (mx - mn) * step_and_output(s);
+}
+/* random.glsl:32-37 */
+static v3 random_in_unit_sphere(uint32_t* s) {
+  float rho = step_and_output(s);
+  float theta = random_range(s, 0.0f, 2.0f * ORC_PI);
+  float phi = random_range(s, 0.0f, ORC_PI);
+  float sp, cp, st, ct;
+  rt_sincos(phi, &sp, &cp);
+  rt_sincos(theta, &st, &ct);
+  return V(rho * sp * ct, rho * sp * st, rho * cp);
+}
+/* random.glsl:59-61 */
+static v3 random_unit_vector(uint32_t* s) { return vnormalize(random_in_unit_sphere(s)); }
+
+/* n draws of random() from state s; writes the floats and the states. */
+void orc_random_stream(uint32_t s, uint32_t n, float* out, uint32_t* states) {
+  for (uint32_t i = 0; i < n; ++i) {
+    out[i] = step_and_output(&s);
+    if (states) states[i] = s;
+  }
+}
+void orc_random_unit_vectors(uint32_t s, uint32_t n, float* out3) {
+  for (uint32_t i = 0; i < n; ++i) {
+    v3 v = random_unit_vector(&s);
+    out3[3 * i] = v.x; out3[3 * i + 1] = v.y; out3[3 * i + 2] = v.z;
+  }
+}
+
+/* ------------------------------------------------------------ camera --- */
+/* raytraceBVH.comp:50-81 and getRay :329-342.  out[0..11] = camPos,
+ * pixel00, pixelDeltaU, pixelDeltaV. */
+void orc_camera(const OUbo* ubo, uint32_t width, uint32_t height, float* out) {
+  float W = (float)width, H = (float)height;
+  float aspect = W / H;
+  float theta = ubo->fov * 0x1.1df46ap-6f;               /* radians() */
+  float h = (float)tan((double)(theta / 2.0f));
+  float vh = 2.0f * h * 10.0f;                           /* _FOCAL_DISTANCE 10 */
+  float vw = vh * aspect;
+  v3 pos = V4(ubo->camPos), look = V4(ubo->camLookAt), up = V4(ubo->camUpDir);
+  v3 w = vnormalize(vsub(pos, look));
+  v3 u = vnormalize(vcross(up, w));
+  v3 v = vcross(w, u);
+  v3 vpu = vscale(u, vw);
+  v3 vpv = vscale(vneg(v), vh);
+  v3 pdu = V(vpu.x / W, vpu.y / W, vpu.z / W);
+  v3 pdv = V(vpv.x / H, vpv.y / H, vpv.z / H);
+  v3 ul = vsub(vsub(vsub(pos, vscale(w, 10.0f)), vdivs(vpu, 2.0f)), vdivs(vpv, 2.0f));
+  v3 p00 = vadd(ul, vscale(vadd(pdu, pdv), 0.5f));
+  float vals[12] = {pos.x, pos.y, pos.z, p00.x, p00.y, p00.z, pdu.x, pdu.y, pdu.z, pdv.x, pdv.y, pdv.z};
+  memcpy(out, vals, sizeof(vals));
+}
+
+static inline v3 camera_dir(const float* cam, uint32_t x, uint32_t y) {
+  v3 pos = V(cam[0], cam[1], cam[2]), p00 = V(cam[3], cam[4], cam[5]);
+  v3 pdu = V(cam[6], cam[7], cam[8]), pdv = V(cam[9], cam[10], cam[11]);
+  float fx = (float)x, fy = (float)y;
+  v3 sample = vadd(vadd(p00, vscale(pdu, fx)), vscale(pdv, fy));
+  return vnormalize(vsub(sample, pos));
+}
+
+/* Primary rays of the first bounce: origin camPos, direction
+ * normalize(getRay().direction) (rayColor re-normalises, :280), interval
+ * [0.001, 1e7] of sceneHit (:268-269). */
+void orc_primary_rays(const OUbo* ubo, uint32_t width, uint32_t height, ORay* out) {
+  float cam[12];
+  orc_camera(ubo, width, height, cam);
+  for (uint32_t y = 0; y < height; ++y)
+    for (uint32_t x = 0; x < width; ++x) {
+      v3 d = vnormalize(camera_dir(cam, x, y));
+      ORay* r = &out[(size_t)y * width + x];
+      r->o[0] = cam[0]; r->o[1] = cam[1]; r->o[2] = cam[2];
+      r->d[0] = d.x; r->d[1] = d.y; r->d[2] = d.z;
+      r->tmin = 0.001f; r->tmax = 10000000.0f;
+    }
+}
+
+/* ------------------------------------------------------ intersections -- */
+typedef struct {
+  v3 p, normal;
+  uint32_t mat;
+  float t;
+  int back;
+  float u, v;
+  uint32_t prim;
+} ORec;
+
+/* raytraceBVH.comp:118-149 */
+static int triangle_hit(const OTri* T, v3 o, v3 d, float tmin, float tmax, ORec* rec) {
+  v3 v0 = V4(T->v0), v1 = V4(T->v1), v2 = V4(T->v2);
+  v3 u = vsub(v1, v0);
+  v3 v = vsub(v2, v0);
+  v3 N = vcross(u, v);
+  v3 n = vnormalize(N);
+  float D = vdot(n, v0);
+  v3 w = vdivs(N, vdot(N, N));
+  float denom = vdot(n, d);
+  if (fabsf(denom) < 0.0001f) return 0;
+  float t = (D - vdot(n, o)) / denom;
+  if (t < tmin || t > tmax) return 0;
+  if (t != t) return 0; /* zero-area triangle: defined as a miss */
+  v3 P = vadd(o, vscale(d, t));
+  v3 q = vsub(P, v0);
+  float a = vdot(w, vcross(q, v));
+  float b = vdot(w, vcross(u, q));
+  if (a < 0.0f || b < 0.0f || a + b > 1.0f) return 0;
+  rec->t = t;
+  rec->p = P;
+  rec->u = a;
+  rec->v = b;
+  rec->back = vdot(d, n) > 0.0f ? 1 : 0;
+  rec->normal = vscale(n, (float)(1 - 2 * rec->back));
+  rec->mat = T->mat;
+  return 1;
+}
+
+/* raytraceBVH.comp:152-181 (u,v of :172-173 are never read on the path) */
+static int sphere_hit(const OSph* S, v3 o, v3 d, float tmin, float tmax, ORec* rec) {
+  v3 C = V4(S->c);
+  v3 oc = vsub(o, C);
+  float a = vdot(d, d);
+  float halfB = vdot(oc, d);
+  float c = vdot(oc, oc) - (S->r * S->r);
+  float under = (halfB * halfB) - (a * c);
+  if (under < 0.0f) return 0;
+  float rad = sqrtf(under);
+  float root = (-halfB - rad) / a;
+  if (root < tmin || root > tmax) {
+    root = (-halfB + rad) / a;
+    if (root < tmin || root > tmax) return 0;
+  }
+  rec->t = root;
+  rec->p = vadd(o, vscale(d, root));
+  rec->u = 0.0f;
+  rec->v = 0.0f;
+  rec->normal = vdivs(vsub(rec->p, C), S->r);
+  rec->back = vdot(d, rec->normal) > 0.0f ? 1 : 0;
+  rec->normal = vscale(rec->normal, (float)(1 - 2 * rec->back));
+  rec->mat = S->mat;
+  return 1;
+}
+
+/* raytraceBVH.comp:184-193 */
+static inline void slab(v3 o, v3 d, const ONode* nd, float* tnear, float* tfar) {
+  float x0 = (nd->minX - o.x) / d.x, y0 = (nd->minY - o.y) / d.y, z0 = (nd->minZ - o.z) / d.z;
+  float x1 = (nd->maxX - o.x) / d.x, y1 = (nd->maxY - o.y) / d.y, z1 = (nd->maxZ - o.z) / d.z;
+  float ax = fminf(x0, x1), ay = fminf(y0, y1), az = fminf(z0, z1);
+  float bx = fmaxf(x0, x1), by = fmaxf(y0, y1), bz = fmaxf(z0, z1);
+  *tnear = fmaxf(fmaxf(ax, ay), az);
+  *tfar = fminf(fminf(bx, by), bz);
+}
+
+typedef struct {
+  uint64_t boxes;    /* node boxes tested */
+  uint64_t tris;     /* triangle tests */
+  uint64_t spheres;  /* sphere tests */
+  uint64_t inner;    /* internal nodes expanded */
+  uint64_t status;   /* bit0 stack overflow, bit1 bad index */
+} OStats;
+
+static int leaf_test(const OScene* S, const ONode* nd, v3 o, v3 d, float tmin, float closest,
+                     ORec* rec, OStats* st) {
+  if (nd->ptype == SPHERE_PRIMITIVE) {
+    if (nd->prim >= S->ns) { st->status |= 2; return 0; }
+    st->spheres++;
+    if (sphere_hit(&S->sph[nd->prim], o, d, tmin, closest, rec)) {
+      rec->prim = nd->prim | SPHERE_BIT;
+      return 1;
+    }
+  } else if (nd->ptype == TRIANGLE_PRIMITIVE) {
+    if (nd->prim >= S->nt) { st->status |= 2; return 0; }
+    st->tris++;
+    if (triangle_hit(&S->tris[nd->prim], o, d, tmin, closest, rec)) {
+      rec->prim = nd->prim;
+      return 1;
+    }
+  }
+  return 0;
+}
+
+/* hitBVH in the reference's order (raytraceBVH.comp:195-265): node 0 first;
+ * on a box hit, a leaf is tested and the stack popped, an internal node
+ * pushes its left child and continues with its right child; no interval
+ * culling; a later candidate at equal t replaces the earlier one. */
+static int hit_bvh_reference(const OScene* S, v3 o, v3 d, float tmin, float tmax, int any,
+                             ORec* rec, OStats* st) {
+  if (S->nn == 0) return 0;
+  int hit = 0;
+  float closest = tmax;
+  uint32_t stack[128];
+  uint32_t sp = 0, cur = 0;
+  for (;;) {
+    if (cur >= S->nn) { st->status |= 2; break; }
+    const ONode* nd = &S->nodes[cur];
+    float tn, tf;
+    st->boxes++;
+    slab(o, d, nd, &tn, &tf);
+    if (tn < tf) {
+      if (nd->left == 0u && nd->right == 0u) {
+        if (leaf_test(S, nd, o, d, tmin, closest, rec, st)) {
+          hit = 1;
+          closest = rec->t;
+          if (any) break;
+        }
+        if (sp == 0) break;
+        cur = stack[--sp];
+      } else {
+        st->inner++;
+        if (sp >= 128u) { st->status |= 1; break; }
+        stack[sp++] = nd->left;
+        cur = nd->right;
+      }
+    } else {
+      if (sp == 0) break;
+      cur = stack[--sp];
+    }
+  }
+  return hit;
+}
+
+/* The canonical traversal used to count work and to check large batches:
+ * the same candidate set and tests, visited nearer-child first, skipping a
+ * box whose interval lies wholly outside [tmin, closest] widened by a margin
+ * far above binary32 rounding of t.  It returns the reference's answer except
+ * on exact ties of t, which the reference breaks by visit order. */
+static int hit_bvh_canonical(const OScene* S, v3 o, v3 d, float tmin, float tmax, int any,
+                             ORec* rec, OStats* st) {
+  if (S->nn == 0) return 0;
+  int hit = 0;
+  float closest = tmax;
+  uint32_t stack[128];
+  uint32_t sp = 0;
+  float tn, tf;
+  const ONode* root = &S->nodes[0];
+  st->boxes++;
+  slab(o, d, root, &tn, &tf);
+  float lo = tmin - (1e-4f * fabsf(tmin) + 1e-5f);
+  if (!(tn < tf) || tf < lo) return 0;
+  uint32_t cur = 0;
+  for (;;) {
+    if (cur >= S->nn) { st->status |= 2; break; }
+    const ONode* nd = &S->nodes[cur];
+    int next_valid = 0;
+    if (nd->left == 0u && nd->right == 0u) {
+      if (leaf_test(S, nd, o, d, tmin, closest, rec, st)) {
+        hit = 1;
+        closest = rec->t;
+        if (any) break;
+      }
+    } else {
+      st->inner++;
+      uint32_t ch[2] = {nd->left, nd->right};
+      float n_[2];
+      int ok[2];
+      float hi = closest + (1e-4f * fabsf(closest) + 1e-5f);
+      for (int k = 0; k < 2; ++k) {
+        if (ch[k] >= S->nn) { st->status |= 2; ok[k] = 0; continue; }
+        float a, b;
+        st->boxes++;
+        slab(o, d, &S->nodes[ch[k]], &a, &b);
+        ok[k] = (a < b) && !(b < lo) && !(a > hi);
+        n_[k] = a;
+      }
+      if (ok[0] && ok[1]) {
+        int nearer = (n_[1] < n_[0]) ? 1 : 0;
+        if (sp >= 128u) { st->status |= 1; break; }
+        stack[sp++] = ch[1 - nearer];
+        cur = ch[nearer];
+        next_valid = 1;
+      } else if (ok[0] || ok[1]) {
+        cur = ok[0] ? ch[0] : ch[1];
+        next_valid = 1;
+      }
+    }
+    if (!next_valid) {
+      if (sp == 0) break;
+      cur = stack[--sp];
+    }
+  }
+  return hit;
+}
+
+/* --------------------------------------------------------- trace batch -- */
+typedef struct {
+  const OScene* S;
+  const ORay* rays;
+  OHit* hits;
+  uint32_t n;
+  int any, canonical;
+  _Atomic uint32_t next;
+  OStats totals;
+  pthread_mutex_t lock;
+} TraceJob;
+
+static void trace_one(const OScene* S, const ORay* r, OHit* h, int any, int canonical, OStats* st) {
+  ORec rec;
+  memset(&rec, 0, sizeof(rec));
+  v3 o = V(r->o[0], r->o[1], r->o[2]), d = V(r->d[0], r->d[1], r->d[2]);
+  int hit = canonical ? hit_bvh_canonical(S, o, d, r->tmin, r->tmax, any, &rec, st)
+                      : hit_bvh_reference(S, o, d, r->tmin, r->tmax, any, &rec, st);
+  if (hit) { h->prim = rec.prim; h->t = rec.t; }
+  else { h->prim = NO_HIT; h->t = INFINITY; }
+}
+
+static void* trace_worker(void* arg) {
+  TraceJob* J = (TraceJob*)arg;
+  OStats st;
+  memset(&st, 0, sizeof(st));
+  for (;;) {
+    uint32_t b = atomic_fetch_add(&J->next, 64u);
+    if (b >= J->n) break;
+    uint32_t e = b + 64u < J->n ? b + 64u : J->n;
+    for (uint32_t i = b; i < e; ++i) trace_one(J->S, &J->rays[i], &J->hits[i], J->any, J->canonical, &st);
+  }
+  pthread_mutex_lock(&J->lock);
+  J->totals.boxes += st.boxes; J->totals.tris += st.tris; J->totals.spheres += st.spheres;
+  J->totals.inner += st.inner; J->totals.status |= st.status;
+  pthread_mutex_unlock(&J->lock);
+  return NULL;
+}
+
+/* Traces n rays.  flags bit0 = any-hit, bit1 = canonical order (else the
+ * reference order).  stats (may be NULL) receives the OStats totals. */
+int orc_trace(const OScene* S, const ORay* rays, uint32_t n, OHit* hits, uint32_t flags,
+              uint32_t nthreads, uint64_t* stats) {
+  TraceJob J;
+  memset(&J, 0, sizeof(J));
+  J.S = S; J.rays = rays; J.hits = hits; J.n = n;
+  J.any = (flags & 1u) != 0; J.canonical = (flags & 2u) != 0;
+  atomic_init(&J.next, 0u);
+  pthread_mutex_init(&J.lock, NULL);
+  if (nthreads <= 1) {
+    trace_worker(&J);
+  } else {
+    pthread_t* th = (pthread_t*)malloc(sizeof(pthread_t) * nthreads);
+    if (!th) return -1;
+    for (uint32_t i = 0; i < nthreads; ++i) pthread_create(&th[i], NULL, trace_worker, &J);
+    for (uint32_t i = 0; i < nthreads; ++i) pthread_join(th[i], NULL);
+    free(th);
+  }
+  pthread_mutex_destroy(&J.lock);
+  if (stats) {
+    stats[0] = J.totals.boxes; stats[1] = J.totals.tris; stats[2] = J.totals.spheres;
+    stats[3] = J.totals.inner; stats[4] = J.totals.status;
+  }
+  return 0;
+}
+
+/* The reference triangle test on one ray (binary32); returns 1 and t on a hit. */
+int orc_triangle_test(const OTri* T, const ORay* r, float tmax, float* t_out) {
+  ORec rec;
+  v3 o = V(r->o[0], r->o[1], r->o[2]), d = V(r->d[0], r->d[1], r->d[2]);
+  if (!triangle_hit(T, o, d, r->tmin, tmax, &rec)) return 0;
+  *t_out = rec.t;
+  return 1;
+}
+
+/* Binary64 ray-plane parameter of the triangle's plane and its barycentric
+ * inside test, from the binary32 inputs: the arbiter of near-ties.
+ * Returns the t (NaN when the ray is parallel); *inside = 1 when the plane
+ * point lies in the triangle. */
+double orc_triangle_t64(const OTri* T, const ORay* r, int* inside) {
+  double v0[3], e1[3], e2[3], o[3], d[3];
+  for (int k = 0; k < 3; ++k) {
+    v0[k] = T->v0[k]; e1[k] = (double)T->v1[k] - v0[k]; e2[k] = (double)T->v2[k] - v0[k];
+    o[k] = r->o[k]; d[k] = r->d[k];
+  }
+  double N[3] = {e1[1] * e2[2] - e1[2] * e2[1], e1[2] * e2[0] - e1[0] * e2[2], e1[0] * e2[1] - e1[1] * e2[0]};
+  double nn = N[0] * N[0] + N[1] * N[1] + N[2] * N[2];
+  double den = N[0] * d[0] + N[1] * d[1] + N[2] * d[2];
+  if (den == 0.0 || nn == 0.0) { *inside = 0; return NAN; }
+  double num = N[0] * (v0[0] - o[0]) + N[1] * (v0[1] - o[1]) + N[2] * (v0[2] - o[2]);
+  double t = num / den;
+  double q[3];
+  for (int k = 0; k < 3; ++k) q[k] = o[k] + t * d[k] - v0[k];
+  double c1[3] = {q[1] * e2[2] - q[2] * e2[1], q[2] * e2[0] - q[0] * e2[2], q[0] * e2[1] - q[1] * e2[0]};
+  double c2[3] = {e1[1] * q[2] - e1[2] * q[1], e1[2] * q[0] - e1[0] * q[2], e1[0] * q[1] - e1[1] * q[0]};
+  double a = (N[0] * c1[0] + N[1] * c1[1] + N[2] * c1[2]) / nn;
+  double b = (N[0] * c2[0] + N[1] * c2[1] + N[2] * c2[2]) / nn;
+  *inside = (a >= 0.0 && b >= 0.0 && a + b <= 1.0);
+  return t;
+}
+
+/* Brute force: every triangle the reference test accepts for ray r, with its
+ * binary32 t; returns the count (at most cap are written). */
+uint32_t orc_all_hits(const OScene* S, const ORay* r, uint32_t* ids, float* ts, uint32_t cap) {
+  uint32_t cnt = 0;
+  for (uint32_t i = 0; i < S->nt; ++i) {
+    float t;
+    if (orc_triangle_test(&S->tris[i], r, r->tmax, &t)) {
+      if (cnt < cap) { ids[cnt] = i; ts[cnt] = t; }
+      cnt++;
+    }
+  }
+  return cnt;
+}
+
+/* ------------------------------------------------------------ shading -- */
+static inline v3 reflect3(v3 v, v3 n) { return vsub(v, vscale(n, 2.0f * vdot(v, n))); }
+
+/* Extended materials, beyond the reference (whose scatter() terminates
+ * METALLIC and DIELECTRIC paths): the standard mirror-with-fuzz and
+ * Snell/Schlick dielectric of Shirley's "Ray Tracing in One Weekend". */
+static int scatter(const OScene* S, int extended, v3 d, const ORec* rec, uint32_t* rng, v3* att,
+                   v3* o_out, v3* d_out) {
+  const OMat* m = &S->mats[rec->mat];
+  if (m->type == DIFFUSE_MATERIAL) { /* raytraceBVH.comp:100-115 */
+    *att = V4(m->albedo);
+    *o_out = rec->p;
+    *d_out = vnormalize(vadd(rec->normal, random_unit_vector(rng)));
+    return 1;
+  }
+  if (!extended) return 0;
+  if (m->type == METALLIC_MATERIAL) {
+    v3 refl = vnormalize(reflect3(d, rec->normal));
+    v3 dir = vnormalize(vadd(refl, vscale(random_unit_vector(rng), m->fuzz)));
+    *att = V4(m->albedo);
+    *o_out = rec->p;
+    *d_out = dir;
+    return vdot(dir, rec->normal) > 0.0f;
+  }
+  if (m->type == DIELECTRIC_MATERIAL) {
+    float ri = rec->back ? m->ior : 1.0f / m->ior;
+    float cosv = fminf(-vdot(d, rec->normal), 1.0f);
+    float sinv = sqrtf(1.0f - cosv * cosv);
+    float r0 = (1.0f - ri) / (1.0f + ri);
+    r0 = r0 * r0;
+    float x = 1.0f - cosv;
+    float x2 = x * x;
+    float refl = r0 + (1.0f - r0) * (x2 * x2 * x);
+    float rnd = step_and_output(rng);
+    v3 dir;
+    if (ri * sinv > 1.0f || refl > rnd) {
+      dir = reflect3(d, rec->normal);
+    } else {
+      v3 perp = vscale(vadd(d, vscale(rec->normal, cosv)), ri);
+      v3 par = vscale(rec->normal, -sqrtf(fabsf(1.0f - vdot(perp, perp))));
+      dir = vadd(perp, par);
+    }
+    *att = V(1.0f, 1.0f, 1.0f);
+    *o_out = rec->p;
+    *d_out = vnormalize(dir);
+    return 1;
+  }
+  return 0;
+}
+
+/* rayColor, raytraceBVH.comp:276-315 */
+static v3 ray_color(const OScene* S, v3 o, v3 d, uint32_t depth, uint32_t* rng, int extended,
+                    v3 bg, OStats* st) {
+  v3 color = V(0.0f, 0.0f, 0.0f);
+  v3 gatt = V(1.0f, 1.0f, 1.0f);
+  v3 co = o, cd = vnormalize(d);
+  for (uint32_t i = 0; i < depth; ++i) {
+    ORec rec;
+    memset(&rec, 0, sizeof(rec));
+    if (!hit_bvh_reference(S, co, cd, 0.001f, 10000000.0f, 0, &rec, st)) {
+      v3 b = extended ? bg : V(0.0f, 0.0f, 0.0f);
+      color = vadd(color, vmul(b, gatt));
+      break;
+    }
+    const OMat* m = &S->mats[rec.mat];
+    v3 em = m->type == LIGHT_MATERIAL ? V4(m->albedo) : V(0.0f, 0.0f, 0.0f);
+    color = vadd(color, vmul(em, gatt));
+    v3 att, no, nd;
+    if (!scatter(S, extended, cd, &rec, rng, &att, &no, &nd)) break;
+    gatt = vmul(gatt, att);
+    co = no;
+    cd = nd;
+  }
+  return color;
+}
+
+typedef struct {
+  const OScene* S;
+  const OUbo* ubo;
+  float* accum;
+  uint32_t W, H, spp;
+  int extended;
+  v3 bg;
+  float cam[12];
+  _Atomic uint32_t next;
+  _Atomic uint64_t status;
+} RenderJob;
+
+/* main(), raytraceBVH.comp:345-375, repeated spp times for one pixel. */
+static void render_pixel(RenderJob* J, uint32_t x, uint32_t y, OStats* st) {
+  float* px = &J->accum[((size_t)y * J->W + x) * 4];
+  for (uint32_t s = 0; s < J->spp; ++s) {
+    uint32_t rng = orc_seed(x, y, J->ubo->randomState);
+    rng += f2u_sat(px[3] * 4294967294.0f);
+    /* :351 stepRNG(rngState) discards its result */
+    float next = step_and_output(&rng);
+    v3 d = camera_dir(J->cam, x, y);
+    v3 o = V(J->cam[0], J->cam[1], J->cam[2]);
+    v3 c = ray_color(J->S, o, d, J->ubo->depth, &rng, J->extended, J->bg, st);
+    px[0] = c.x + px[0];
+    px[1] = c.y + px[1];
+    px[2] = c.z + px[2];
+    px[3] = next;
+  }
+}
+
+static void* render_worker(void* arg) {
+  RenderJob* J = (RenderJob*)arg;
+  OStats st;
+  memset(&st, 0, sizeof(st));
+  uint32_t total = J->W * J->H;
+  for (;;) {
+    uint32_t b = atomic_fetch_add(&J->next, 16u);
+    if (b >= total) break;
+    uint32_t e = b + 16u < total ? b + 16u : total;
+    for (uint32_t i = b; i < e; ++i) render_pixel(J, i % J->W, i / J->W, &st);
+  }
+  atomic_fetch_or(&J->status, st.status);
+  return NULL;
+}
+
+/* spp samples per pixel into accum (W*H*4 floats, caller-initialised). */
+int orc_render(const OScene* S, const OUbo* ubo, float* accum, uint32_t W, uint32_t H, uint32_t spp,
+               uint32_t extended, const float* bg, uint32_t nthreads) {
+  RenderJob J;
+  memset(&J, 0, sizeof(J));
+  J.S = S; J.ubo = ubo; J.accum = accum; J.W = W; J.H = H; J.spp = spp;
+  J.extended = extended != 0;
+  J.bg = bg ? V(bg[0], bg[1], bg[2]) : V(0.0f, 0.0f, 0.0f);
+  orc_camera(ubo, W, H, J.cam);
+  atomic_init(&J.next, 0u);
+  atomic_init(&J.status, 0u);
+  if (nthreads <= 1) {
+    render_worker(&J);
+  } else {
+    pthread_t* th = (pthread_t*)malloc(sizeof(pthread_t) * nthreads);
+    if (!th) return -1;
+    for (uint32_t i = 0; i < nthreads; ++i) pthread_create(&th[i], NULL, render_worker, &J);
+    for (uint32_t i = 0; i < nthreads; ++i) pthread_join(th[i], NULL);
+    free(th);
+  }
+  return (int)atomic_load(&J.status);
+}
+
+/* SingleTriangleFullScreen.frag:13-18 */
+void orc_resolve(const float* accum, uint32_t W, uint32_t H, uint32_t spp, float* out) {
+  for (size_t i = 0; i < (size_t)W * H; ++i) {
+    for (int k = 0; k < 3; ++k) {
+      float v = sqrtf(accum[i * 4 + k] / (float)spp);
+      out[i * 4 + k] = fminf(fmaxf(v, 0.0f), 1.0f);
+    }
+    out[i * 4 + 3] = 1.0f;
+  }
+}
+
+/* ---------------------------------------------------------- BVH build -- */
+static const float ORC_DELTA = 0.001f;           /* ConstructHLBVH.comp:38-39 */
+
+static inline void pad_axis(float* mn, float* mx) {
+  const float PADDING = ORC_DELTA / 2.0f;
+  if (*mx - *mn < ORC_DELTA) { *mn -= PADDING; *mx += PADDING; }
+}
+
+/* GenerateMortonCodesOfPrimitives.comp:41-50 */
+uint32_t orc_separate_bits_by_3(uint32_t val) {
+  if (val == 1024u) val--;
+  val = (val | (val << 16)) & 50331903u;
+  val = (val | (val << 8)) & 50393103u;
+  val = (val | (val << 4)) & 51130563u;
+  val = (val | (val << 2)) & 153391689u;
+  return val;
+}
+
+/* ConstructHLBVH.comp:58-70 */
+static int clz_diff(const uint32_t* codes, int n, int i, int j) {
+  if (j < 0 || j > n - 1) return -1;
+  uint32_t ci = codes[i], cj = codes[j];
+  if (ci == cj) return 32 + __builtin_clz((uint32_t)i ^ (uint32_t)j);
+  return __builtin_clz(ci ^ cj);
+}
+
+/* ConstructHLBVH.comp:72-96 */
+static void determine_range(const uint32_t* codes, int n, int id, int* lower, int* upper) {
+  int dl = clz_diff(codes, n, id, id - 1);
+  int dr = clz_diff(codes, n, id, id + 1);
+  int dir = (dr >= dl) ? 1 : -1;
+  int dmin = dl < dr ? dl : dr;
+  int lmax = 2;
+  while (clz_diff(codes, n, id, id + lmax * dir) > dmin) lmax <<= 1;
+  int l = 0;
+  for (int t = lmax >> 1; t > 0; t >>= 1)
+    if (clz_diff(codes, n, id, id + (l + t) * dir) > dmin) l += t;
+  int end = id + l * dir;
+  *lower = id < end ? id : end;
+  *upper = id > end ? id : end;
+}
+
+/* ConstructHLBVH.comp:98-115 */
+static int find_split(const uint32_t* codes, int n, int first, int last) {
+  int common = clz_diff(codes, n, first, last);
+  int split = first;
+  int stride = last - first;
+  do {
+    stride = (stride + 1) >> 1;
+    int ns = split + stride;
+    if (ns < last) {
+      if (clz_diff(codes, n, first, ns) > common) split = ns;
+    }
+  } while (stride > 1);
+  return split;
+}
+
+/* Karras tree over sorted codes alone (ConstructHLBVH.comp:171-209), for the
+ * published worked example: left/right child of internal node i, leaves
+ * encoded as n-1+k. */
+void orc_karras(const uint32_t* codes, uint32_t n, uint32_t* left, uint32_t* right) {
+  int N = (int)n;
+  for (int i = 0; i < N - 1; ++i) {
+    int first, last;
+    determine_range(codes, N, i, &first, &last);
+    int split = find_split(codes, N, first, last);
+    left[i] = (uint32_t)(split == first ? (N - 1) + split : split);
+    right[i] = (uint32_t)(split + 1 == last ? (N - 1) + split + 1 : split + 1);
+  }
+}
+
+typedef struct { uint32_t code, prim, type; } OMorton;
+
+/* Builds the 2N-1 node array exactly as the six S1 passes do.
+ * mode 0 = sorted (corrected), 1 = reference.  models may be NULL.
+ * Optional outputs: sorted codes[N], sorted prims (type<<31 | index)[N],
+ * enclosing[6] = padded centroid box (minxyz, maxxyz). */
+int orc_build_bvh(const OTri* tris_in, uint32_t nt, const OSph* sph_in, uint32_t ns,
+                  const float* models, uint32_t nmodels, uint32_t mode, ONode* out,
+                  uint32_t* out_codes, uint32_t* out_prims, float* out_enclosing) {
+  uint32_t N = nt + ns;
+  if (N == 0) return 0;
+  OTri* tris = (OTri*)malloc(sizeof(OTri) * (nt ? nt : 1));
+  OSph* sph = (OSph*)malloc(sizeof(OSph) * (ns ? ns : 1));
+  OMorton* mp = (OMorton*)malloc(sizeof(OMorton) * N);
+  OMorton* tmp = (OMorton*)malloc(sizeof(OMorton) * N);
+  uint32_t* codes = (uint32_t*)malloc(sizeof(uint32_t) * N);
+  uint32_t* parent = (uint32_t*)calloc(2 * N - 1, sizeof(uint32_t));
+  int* visits = (int*)calloc(2 * N - 1, sizeof(int));
+  if (!tris || !sph || !mp || !tmp || !codes || !parent || !visits) return -1;
+  if (nt) memcpy(tris, tris_in, sizeof(OTri) * nt);
+  if (ns) memcpy(sph, sph_in, sizeof(OSph) * ns);
+
+  /* pass 1: ModelSpaceToWorldSpace.comp:32-48, v' = M * vec4(v, 1) */
+  if (models) {
+    for (uint32_t i = 0; i < nt; ++i) {
+      if (tris[i].model >= nmodels) return -2;
+      const float* m = &models[16 * tris[i].model];
+      float* vs[3] = {tris[i].v0, tris[i].v1, tris[i].v2};
+      for (int k = 0; k < 3; ++k) {
+        float x = vs[k][0], y = vs[k][1], z = vs[k][2], w = 1.0f;
+        float r[4];
+        for (int row = 0; row < 4; ++row)
+          r[row] = m[0 + row] * x + m[4 + row] * y + m[8 + row] * z + m[12 + row] * w;
+        memcpy(vs[k], r, sizeof(r));
+      }
+    }
+    for (uint32_t i = 0; i < ns; ++i) {
+      if (sph[i].model >= nmodels) return -2;
+      const float* m = &models[16 * sph[i].model];
+      float x = sph[i].c[0], y = sph[i].c[1], z = sph[i].c[2], w = 1.0f;
+      float r[4];
+      for (int row = 0; row < 4; ++row)
+        r[row] = m[0 + row] * x + m[4 + row] * y + m[8 + row] * z + m[12 + row] * w;
+      memcpy(sph[i].c, r, sizeof(r));
+    }
+  }
+
+  /* centroids (GetEnclosingAABB.comp:40-42; spheres use their centre) */
+  float (*cen)[3] = (float (*)[3])malloc(sizeof(float) * 3 * N);
+  if (!cen) return -1;
+  for (uint32_t i = 0; i < N; ++i) {
+    if (i < nt) {
+      for (int k = 0; k < 3; ++k)
+        cen[i][k] = (tris[i].v0[k] + tris[i].v1[k] + tris[i].v2[k]) / 3.0f;
+    } else {
+      for (int k = 0; k < 3; ++k) cen[i][k] = sph[i - nt].c[k];
+    }
+  }
+
+  /* pass 2: GetEnclosingAABB.comp:64-109 */
+  float emin[3] = {1000000000.0f, 1000000000.0f, 1000000000.0f};
+  float emax[3] = {-1000000000.0f, -1000000000.0f, -1000000000.0f};
+  for (uint32_t i = 0; i < N; ++i)
+    for (int k = 0; k < 3; ++k) {
+      emin[k] = fminf(emin[k], cen[i][k]);
+      emax[k] = fmaxf(emax[k], cen[i][k]);
+    }
+  for (int k = 0; k < 3; ++k) pad_axis(&emin[k], &emax[k]);
+  if (out_enclosing)
+    for (int k = 0; k < 3; ++k) { out_enclosing[k] = emin[k]; out_enclosing[3 + k] = emax[k]; }
+
+  /* pass 3: GenerateMortonCodesOfPrimitives.comp:52-93 */
+  for (uint32_t i = 0; i < N; ++i) {
+    uint32_t q[3];
+    for (int k = 0; k < 3; ++k) {
+      float span = emax[k] - emin[k];
+      float off = mode == 1u ? cen[i][k] / span : (cen[i][k] - emin[k]) / span;
+      q[k] = f2u_sat(off * 1024.0f);
+    }
+    mp[i].code = (orc_separate_bits_by_3(q[2]) << 2) | (orc_separate_bits_by_3(q[1]) << 1) |
+                 orc_separate_bits_by_3(q[0]);
+    mp[i].prim = i < nt ? i : i - nt;
+    mp[i].type = i < nt ? TRIANGLE_PRIMITIVE : SPHERE_PRIMITIVE;
+  }
+
+  /* pass 4: RadixSortSimple.comp:59-157, 4 stable passes of 8 bits */
+  for (uint32_t it = 0; it < 4; ++it) {
+    uint32_t shift = 8u * it, hist[256], off[256];
+    memset(hist, 0, sizeof(hist));
+    for (uint32_t i = 0; i < N; ++i) hist[(mp[i].code >> shift) & 255u]++;
+    uint32_t acc = 0;
+    for (int b = 0; b < 256; ++b) { off[b] = acc; acc += hist[b]; }
+    for (uint32_t i = 0; i < N; ++i) tmp[off[(mp[i].code >> shift) & 255u]++] = mp[i];
+    OMorton* sw = mp; mp = tmp; tmp = sw;
+  }
+  for (uint32_t i = 0; i < N; ++i) codes[i] = mp[i].code;
+  if (out_codes) memcpy(out_codes, codes, sizeof(uint32_t) * N);
+  if (out_prims)
+    for (uint32_t i = 0; i < N; ++i) out_prims[i] = (mp[i].type == SPHERE_PRIMITIVE ? SPHERE_BIT : 0u) | mp[i].prim;
+
+  /* pass 5: ConstructHLBVH.comp:145-214 */
+  uint32_t leaf_off = N - 1;
+  for (uint32_t i = 0; i < N; ++i) {
+    uint32_t type, prim;
+    if (mode == 1u) { /* reference: leaf i holds primitive i (:152-169) */
+      type = i < nt ? TRIANGLE_PRIMITIVE : SPHERE_PRIMITIVE;
+      prim = i < nt ? i : i - nt;
+    } else { /* sorted: leaf i holds the i-th sorted primitive */
+      type = mp[i].type;
+      prim = mp[i].prim;
+    }
+    ONode* nd = &out[leaf_off + i];
+    if (type == TRIANGLE_PRIMITIVE) { /* :132-143 */
+      const OTri* t = &tris[prim];
+      nd->minX = fminf(t->v0[0], fminf(t->v1[0], t->v2[0]));
+      nd->maxX = fmaxf(t->v0[0], fmaxf(t->v1[0], t->v2[0]));
+      nd->minY = fminf(t->v0[1], fminf(t->v1[1], t->v2[1]));
+      nd->maxY = fmaxf(t->v0[1], fmaxf(t->v1[1], t->v2[1]));
+      nd->minZ = fminf(t->v0[2], fminf(t->v1[2], t->v2[2]));
+      nd->maxZ = fmaxf(t->v0[2], fmaxf(t->v1[2], t->v2[2]));
+    } else { /* :117-130 */
+      const OSph* s = &sph[prim];
+      float l[3], r[3];
+      for (int k = 0; k < 3; ++k) { l[k] = s->c[k] - s->r; r[k] = s->c[k] + s->r; }
+      nd->minX = fminf(l[0], r[0]); nd->maxX = fmaxf(l[0], r[0]);
+      nd->minY = fminf(l[1], r[1]); nd->maxY = fmaxf(l[1], r[1]);
+      nd->minZ = fminf(l[2], r[2]); nd->maxZ = fmaxf(l[2], r[2]);
+    }
+    pad_axis(&nd->minX, &nd->maxX);
+    pad_axis(&nd->minY, &nd->maxY);
+    pad_axis(&nd->minZ, &nd->maxZ);
+    nd->left = 0; nd->right = 0; nd->prim = prim; nd->ptype = type;
+  }
+  for (int i = 0; i < (int)N - 1; ++i) {
+    int first, last;
+    determine_range(codes, (int)N, i, &first, &last);
+    int split = find_split(codes, (int)N, first, last);
+    uint32_t lc = (uint32_t)(split == first ? (int)leaf_off + split : split);
+    uint32_t rc = (uint32_t)(split + 1 == last ? (int)leaf_off + split + 1 : split + 1);
+    ONode* nd = &out[i];
+    nd->minX = nd->maxX = nd->minY = nd->maxY = nd->minZ = nd->maxZ = 0.0f;
+    nd->left = lc; nd->right = rc; nd->prim = 0; nd->ptype = 0;
+    parent[lc] = (uint32_t)i;
+    parent[rc] = (uint32_t)i;
+  }
+  parent[0] = 0;
+
+  /* pass 6: ConstructAABBsOfInternalNodes.comp:38-64; the second child to
+   * arrive computes the union, so a serial walk in leaf order is exact. */
+  for (uint32_t i = 0; i < N; ++i) {
+    uint32_t node = parent[leaf_off + i];
+    if (N == 1) break;
+    for (;;) {
+      int v = visits[node]++;
+      if (v < 1) break;
+      ONode* nd = &out[node];
+      const ONode* l = &out[nd->left];
+      const ONode* r = &out[nd->right];
+      nd->minX = fminf(l->minX, r->minX); nd->maxX = fmaxf(l->maxX, r->maxX);
+      nd->minY = fminf(l->minY, r->minY); nd->maxY = fmaxf(l->maxY, r->maxY);
+      nd->minZ = fminf(l->minZ, r->minZ); nd->maxZ = fmaxf(l->maxZ, r->maxZ);
+      if (node == 0) break;
+      node = parent[node];
+    }
+  }
+  free(tris); free(sph); free(mp); free(tmp); free(codes); free(parent); free(visits); free(cen);
+  return 0;
+}
+
+uint32_t orc_abi(void) { return 1u; }

@@ -1,0 +1,338 @@
+"""GB300 (sm_103a) ray-tracing hot path of RaytracerGPU_MastersProject.
+
+Python host mirror of the C ABI in include/rt_gb300.h.  The reference's host
+interface for this path is the raytrace pass of RaytracerBVHRenderer::Raytracer
+(RaytracerBVH.hpp:206-496): a RaytraceScene whose triangle, sphere, material
+and BVH-node buffers, plus a ParameterUBO and an RGBA32F accumulator, feed one
+compute dispatch per ray per pixel.  Here:
+
+  Scene(...)        RaytraceScene::prepForRender + S1 BVH build  (rt_scene_create_ex)
+  Scene.trace(...)  hitBVH over a batch of rays                    (rt_trace)
+  Scene.render(...) the S2 pass, spp samples into the accumulator  (rt_render)
+
+Every call goes to librt_gb300.so.  There is no CPU fallback: importing this
+package without the built library raises, and so does calling a GPU entry
+point without a GPU.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from pathlib import Path
+
+import numpy as np
+
+_PKG = Path(__file__).resolve().parent
+LIB_PATH = _PKG / "librt_gb300.so"
+
+# ------------------------------------------------------------------ records
+TRIANGLE_DTYPE = np.dtype([("v0", "<f4", 4), ("v1", "<f4", 4), ("v2", "<f4", 4), ("materialIndex", "<u4"),
+                           ("modelIndex", "<u4"), ("_pad", "<u4", 2)])
+SPHERE_DTYPE = np.dtype([("center", "<f4", 4), ("radius", "<f4"), ("materialIndex", "<u4"),
+                         ("modelIndex", "<u4"), ("_pad", "<u4")])
+MATERIAL_DTYPE = np.dtype([("albedo", "<f4", 4), ("materialType", "<u4"), ("fuzz", "<f4"), ("ior", "<f4"),
+                           ("_pad", "<u4")])
+NODE_DTYPE = np.dtype([("minX", "<f4"), ("maxX", "<f4"), ("minY", "<f4"), ("maxY", "<f4"), ("minZ", "<f4"),
+                       ("maxZ", "<f4"), ("left", "<u4"), ("right", "<u4"), ("primitiveIndex", "<u4"),
+                       ("primitiveType", "<u4")])
+MODEL_DTYPE = np.dtype([("m", "<f4", 16)])
+RAY_DTYPE = np.dtype([("org", "<f4", 3), ("tmin", "<f4"), ("dir", "<f4", 3), ("tmax", "<f4")])
+HIT_DTYPE = np.dtype([("prim", "<u4"), ("t", "<f4")])
+assert TRIANGLE_DTYPE.itemsize == 64 and SPHERE_DTYPE.itemsize == 32 and MATERIAL_DTYPE.itemsize == 32
+assert NODE_DTYPE.itemsize == 40 and RAY_DTYPE.itemsize == 32 and HIT_DTYPE.itemsize == 8
+
+MAT_LIGHT, MAT_DIFFUSE, MAT_METALLIC, MAT_DIELECTRIC = 0, 1, 2, 3
+PRIM_SPHERE, PRIM_TRIANGLE = 0, 1
+BVH_SORTED, BVH_REFERENCE = 0, 1
+TRACE_CLOSEST, TRACE_ANY = 0, 1
+SHADE_REFERENCE, SHADE_EXTENDED = 0, 1
+NO_HIT = 0xFFFFFFFF
+HIT_SPHERE_BIT = 0x80000000
+
+STATUS = {0: "RT_OK", 1: "RT_EINVAL", 2: "RT_ENOMEM", 3: "RT_ETIMEOUT", 4: "RT_ESTACK", 5: "RT_ECUDA",
+          6: "RT_EBUSY", 7: "RT_ECANCELED", 8: "RT_ENOTFOUND", 9: "RT_EUNSUPPORTED"}
+
+
+class RtError(RuntimeError):
+    def __init__(self, status: int, where: str, msg: str):
+        self.status = status
+        super().__init__(f"{where}: {STATUS.get(status, status)}: {msg}")
+
+
+class RaytracingUBO(C.Structure):
+    """ParameterUBO (raytraceBVH.comp:7-18; RaytracerBVH.hpp:31-42), 80 bytes."""
+    _fields_ = [("camPos", C.c_float * 4), ("camLookAt", C.c_float * 4), ("camUpDir", C.c_float * 4),
+                ("verticalFOV", C.c_float), ("numTriangles", C.c_uint32), ("numSpheres", C.c_uint32),
+                ("numMaterials", C.c_uint32), ("numLights", C.c_uint32), ("maxRayTraceDepth", C.c_uint32),
+                ("randomState", C.c_uint32), ("_pad", C.c_uint32)]
+
+
+class _SceneDesc(C.Structure):
+    _fields_ = [("triangles", C.c_void_p), ("num_triangles", C.c_uint32), ("spheres", C.c_void_p),
+                ("num_spheres", C.c_uint32), ("materials", C.c_void_p), ("num_materials", C.c_uint32),
+                ("models", C.c_void_p), ("num_models", C.c_uint32), ("nodes", C.c_void_p),
+                ("num_nodes", C.c_uint32), ("bvh_mode", C.c_uint32), ("leaf_size", C.c_uint32)]
+
+
+class SceneInfo(C.Structure):
+    _fields_ = [("num_triangles", C.c_uint32), ("num_spheres", C.c_uint32), ("num_materials", C.c_uint32),
+                ("num_nodes", C.c_uint32), ("device_nodes", C.c_uint32), ("depth", C.c_uint32),
+                ("leaf_size", C.c_uint32), ("bvh_mode", C.c_uint32), ("device_bytes", C.c_uint64),
+                ("build_seconds", C.c_double)]
+
+
+class _RenderOptions(C.Structure):
+    _fields_ = [("shade_mode", C.c_uint32), ("background", C.c_float * 3)]
+
+
+assert C.sizeof(RaytracingUBO) == 80
+
+# ------------------------------------------------------------------ loading
+_lib = None
+
+# Every symbol the library must export, with (restype, argtypes).
+_P, _U32, _U64, _F, _D, _I = C.c_void_p, C.c_uint32, C.c_uint64, C.c_float, C.c_double, C.c_int
+SIGNATURES = {
+    "rt_scene_create": (_I, [_P, _U32, _P, _U32, _P, _U32, _P, C.POINTER(C.c_void_p)]),
+    "rt_scene_create_ex": (_I, [C.POINTER(_SceneDesc), C.POINTER(C.c_void_p)]),
+    "rt_scene_destroy": (_I, [_P]),
+    "rt_scene_get_info": (_I, [_P, C.POINTER(SceneInfo)]),
+    "rt_scene_get_nodes": (_I, [_P, _P, _U32]),
+    "rt_build_bvh": (_I, [_P, _U32, _P, _U32, _P, _U32, _U32, _P]),
+    "rt_trace": (_I, [_P, _P, _U32, _P, _U32, _P]),
+    "rt_trace_host": (_I, [_P, _P, _U32, _P, _U32, _P]),
+    "rt_render": (_I, [_P, C.POINTER(RaytracingUBO), _P, _U32, _U32, _U32, C.POINTER(_RenderOptions), _P]),
+    "rt_accum_clear": (_I, [_P, _U32, _U32, _P]),
+    "rt_resolve": (_I, [_P, _U32, _U32, _U32, _P, _P]),
+    "rt_last_error_string": (C.c_char_p, []),
+    "rt_abi_version": (_U32, []),
+    "rt_stream_wait": (_I, [_P, _D]),
+    "rt_gen_uniform": (_I, [_U64, _U64, _U64, _P]),
+    "rt_gen_icosphere": (_I, [_U32, _P, _F, _U32, _P, _U64, C.POINTER(_U64)]),
+    "rt_gen_config1": (_I, [_P, C.POINTER(RaytracingUBO), _P]),
+    "rt_gen_camera_rays": (_I, [C.POINTER(RaytracingUBO), _U32, _U32, _P]),
+    "rt_gen_soup": (_I, [_U64, _U64, _U32, _F, _F, _U32, _P]),
+    "rt_gen_rays": (_I, [_U64, _U64, _U32, _F, _F, _F, _P]),
+    "rt_gen_spheres_scene": (_I, [_U64, _U32, _U32, _F, _P, _P]),
+}
+
+
+def lib() -> C.CDLL:
+    """Loads librt_gb300.so (built by __graft_entry__.build()); raises if absent."""
+    global _lib
+    if _lib is None:
+        path = Path(os.environ.get("RT_GB300_LIB", LIB_PATH))
+        if not path.exists():
+            raise ImportError(f"{path} is not built: run python -c 'import __graft_entry__ as g; g.build()'")
+        L = C.CDLL(str(path))
+        for name, (res, args) in SIGNATURES.items():
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = L
+    return _lib
+
+
+def _check(status: int, where: str) -> None:
+    if status != 0:
+        raise RtError(status, where, lib().rt_last_error_string().decode(errors="replace"))
+
+
+def _ptr(a) -> int | None:
+    """Address of a numpy array or torch tensor (None for None/empty)."""
+    if a is None:
+        return None
+    if isinstance(a, np.ndarray):
+        if a.size == 0:
+            return None
+        assert a.flags["C_CONTIGUOUS"], "arrays passed to the ABI must be C-contiguous"
+        return a.ctypes.data
+    if hasattr(a, "data_ptr"):
+        assert a.is_contiguous(), "tensors passed to the ABI must be contiguous"
+        return a.data_ptr() or None
+    raise TypeError(f"cannot take the address of {type(a)}")
+
+
+def _stream_handle(stream) -> int | None:
+    if stream is None:
+        try:
+            import torch
+            if torch.cuda.is_available():
+                return torch.cuda.current_stream().cuda_stream or None
+        except ImportError:
+            pass
+        return None
+    if isinstance(stream, int):
+        return stream or None
+    return stream.cuda_stream or None
+
+
+# ------------------------------------------------------------------- scene
+class Scene:
+    """A scene resident on the device: RaytraceScene's buffers + the BVH.
+
+    triangles: TRIANGLE_DTYPE array (world space unless models is given)
+    spheres, materials, models, nodes: optional arrays of the record dtypes
+    bvh_mode: BVH_SORTED (default) or BVH_REFERENCE (the reference's leaf order)
+    leaf_size: max triangles per device leaf (1..8); 0 = library default
+    """
+
+    def __init__(self, triangles, spheres=None, materials=None, models=None, nodes=None,
+                 bvh_mode: int = BVH_SORTED, leaf_size: int = 0):
+        L = lib()
+        tri = np.ascontiguousarray(triangles, dtype=TRIANGLE_DTYPE) if triangles is not None else np.zeros(0, TRIANGLE_DTYPE)
+        sph = np.ascontiguousarray(spheres, dtype=SPHERE_DTYPE) if spheres is not None else np.zeros(0, SPHERE_DTYPE)
+        mat = np.ascontiguousarray(materials, dtype=MATERIAL_DTYPE) if materials is not None else np.zeros(0, MATERIAL_DTYPE)
+        mod = np.ascontiguousarray(models, dtype=MODEL_DTYPE) if models is not None else None
+        nod = np.ascontiguousarray(nodes, dtype=NODE_DTYPE) if nodes is not None else None
+        d = _SceneDesc(_ptr(tri), len(tri), _ptr(sph), len(sph), _ptr(mat), len(mat),
+                       _ptr(mod), 0 if mod is None else len(mod), _ptr(nod), 0 if nod is None else len(nod),
+                       bvh_mode, leaf_size)
+        h = C.c_void_p()
+        _check(L.rt_scene_create_ex(C.byref(d), C.byref(h)), "rt_scene_create_ex")
+        self._h = h
+        self.num_triangles = len(tri)
+        self.num_spheres = len(sph)
+
+    @property
+    def handle(self) -> int:
+        if self._h is None:
+            raise ValueError("scene destroyed")
+        return self._h.value
+
+    def info(self) -> SceneInfo:
+        inf = SceneInfo()
+        _check(lib().rt_scene_get_info(self.handle, C.byref(inf)), "rt_scene_get_info")
+        return inf
+
+    def nodes(self) -> np.ndarray:
+        n = self.info().num_nodes
+        out = np.zeros(n, NODE_DTYPE)
+        _check(lib().rt_scene_get_nodes(self.handle, _ptr(out), n), "rt_scene_get_nodes")
+        return out
+
+    def trace(self, rays, hits, n: int | None = None, any_hit: bool = False, stream=None) -> None:
+        """rays/hits: device tensors holding RtRay / RtHit records (stream-ordered)."""
+        if n is None:
+            n = rays.numel() * rays.element_size() // RAY_DTYPE.itemsize
+        _check(lib().rt_trace(self.handle, _ptr(rays), n, _ptr(hits), TRACE_ANY if any_hit else TRACE_CLOSEST,
+                              _stream_handle(stream)), "rt_trace")
+
+    def trace_host(self, rays: np.ndarray, any_hit: bool = False, out: np.ndarray | None = None, stream=None) -> np.ndarray:
+        """Host rays in, host hits out; copies overlap with tracing inside the library."""
+        rays = np.ascontiguousarray(rays, dtype=RAY_DTYPE)
+        if out is None:
+            out = np.empty(len(rays), HIT_DTYPE)
+        _check(lib().rt_trace_host(self.handle, _ptr(rays), len(rays), _ptr(out),
+                                   TRACE_ANY if any_hit else TRACE_CLOSEST, _stream_handle(stream)), "rt_trace_host")
+        return out
+
+    def render(self, ubo: RaytracingUBO, accum, width: int, height: int, spp: int,
+               shade_mode: int = SHADE_REFERENCE, background=(0.0, 0.0, 0.0), stream=None) -> None:
+        """accum: device float32 tensor of width*height*4 (RGBA32F, alpha = RNG carry)."""
+        opt = _RenderOptions(shade_mode, (C.c_float * 3)(*background))
+        _check(lib().rt_render(self.handle, C.byref(ubo), _ptr(accum), width, height, spp, C.byref(opt),
+                               _stream_handle(stream)), "rt_render")
+
+    def close(self) -> None:
+        if getattr(self, "_h", None) is not None and self._h.value:
+            lib().rt_scene_destroy(self._h.value)
+        self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+
+def build_bvh(triangles, spheres=None, models=None, bvh_mode: int = BVH_SORTED) -> np.ndarray:
+    """Host BVH build alone (the six S1 passes) -> NODE_DTYPE array of 2N-1 nodes."""
+    tri = np.ascontiguousarray(triangles, dtype=TRIANGLE_DTYPE)
+    sph = np.ascontiguousarray(spheres, dtype=SPHERE_DTYPE) if spheres is not None else np.zeros(0, SPHERE_DTYPE)
+    mod = np.ascontiguousarray(models, dtype=MODEL_DTYPE) if models is not None else None
+    n = len(tri) + len(sph)
+    out = np.zeros(max(2 * n - 1, 0), NODE_DTYPE)
+    _check(lib().rt_build_bvh(_ptr(tri), len(tri), _ptr(sph), len(sph), _ptr(mod), 0 if mod is None else len(mod),
+                              bvh_mode, _ptr(out)), "rt_build_bvh")
+    return out
+
+
+def accum_clear(accum, width: int, height: int, stream=None) -> None:
+    _check(lib().rt_accum_clear(_ptr(accum), width, height, _stream_handle(stream)), "rt_accum_clear")
+
+
+def resolve(accum, width: int, height: int, spp: int, out, stream=None) -> None:
+    _check(lib().rt_resolve(_ptr(accum), width, height, spp, _ptr(out), _stream_handle(stream)), "rt_resolve")
+
+
+# --------------------------------------------------------------- workloads
+def gen_uniform(seed: int, stream: int, n: int) -> np.ndarray:
+    out = np.empty(n, np.float64)
+    _check(lib().rt_gen_uniform(seed, stream, n, _ptr(out)), "rt_gen_uniform")
+    return out
+
+
+def gen_icosphere(subdiv: int, center=(0.0, 0.0, 0.0), radius: float = 1.0, material: int = 0) -> np.ndarray:
+    n = 20 * 4 ** subdiv
+    out = np.zeros(n, TRIANGLE_DTYPE)
+    c = (C.c_float * 3)(*center)
+    cnt = C.c_uint64()
+    _check(lib().rt_gen_icosphere(subdiv, C.cast(c, C.c_void_p), radius, material, _ptr(out), n, C.byref(cnt)),
+           "rt_gen_icosphere")
+    return out
+
+
+def gen_config1():
+    """-> (triangles[20482], ubo, rays[640*360])"""
+    tris = np.zeros(20482, TRIANGLE_DTYPE)
+    rays = np.zeros(640 * 360, RAY_DTYPE)
+    ubo = RaytracingUBO()
+    _check(lib().rt_gen_config1(_ptr(tris), C.byref(ubo), _ptr(rays)), "rt_gen_config1")
+    return tris, ubo, rays
+
+
+def gen_camera_rays(ubo: RaytracingUBO, width: int, height: int) -> np.ndarray:
+    out = np.zeros(width * height, RAY_DTYPE)
+    _check(lib().rt_gen_camera_rays(C.byref(ubo), width, height, _ptr(out)), "rt_gen_camera_rays")
+    return out
+
+
+def gen_soup(seed: int, stream: int, n: int, side: float = 1.0, sigma: float = 0.002, material: int = 0) -> np.ndarray:
+    out = np.zeros(n, TRIANGLE_DTYPE)
+    _check(lib().rt_gen_soup(seed, stream, n, side, sigma, material, _ptr(out)), "rt_gen_soup")
+    return out
+
+
+def gen_rays(seed: int, stream: int, n: int, side: float = 1.0, tmin: float = 1e-4,
+             tmax: float = float("inf")) -> np.ndarray:
+    out = np.zeros(n, RAY_DTYPE)
+    _check(lib().rt_gen_rays(seed, stream, n, side, tmin, tmax, _ptr(out)), "rt_gen_rays")
+    return out
+
+
+def gen_spheres_scene(seed: int, count: int, subdiv: int, amp: float = 0.05):
+    """-> (triangles, materials) of config 2's displaced icospheres."""
+    tris = np.zeros(count * 20 * 4 ** subdiv, TRIANGLE_DTYPE)
+    mats = np.zeros(count, MATERIAL_DTYPE)
+    _check(lib().rt_gen_spheres_scene(seed, count, subdiv, amp, _ptr(tris), _ptr(mats)), "rt_gen_spheres_scene")
+    return tris, mats
+
+
+def make_ubo(cam_pos, look_at, up=(0.0, 1.0, 0.0), fov: float = 60.0, depth: int = 8, random_state: int = 0,
+             num_triangles: int = 0, num_spheres: int = 0, num_materials: int = 0) -> RaytracingUBO:
+    u = RaytracingUBO()
+    u.camPos[:3] = list(cam_pos)
+    u.camLookAt[:3] = list(look_at)
+    u.camUpDir[:3] = list(up)
+    u.verticalFOV = fov
+    u.numTriangles, u.numSpheres, u.numMaterials = num_triangles, num_spheres, num_materials
+    u.maxRayTraceDepth = depth
+    u.randomState = random_state
+    return u

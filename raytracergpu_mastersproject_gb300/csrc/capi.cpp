@@ -1,0 +1,413 @@
+// capi.cpp -- the extern "C" entry points of include/rt_gb300.h.
+//
+// Ownership: a scene owns one device allocation holding every array of its
+// device form (see rt_internal.h) and a host copy of its reference-layout
+// nodes.  Per-stream work counters (the persistent kernels' ray/pixel
+// queues) live in a small per-(device, stream) workspace created on first use.
+#include <chrono>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <thread>
+
+#include <cuda_runtime.h>
+
+#include "rt_internal.h"
+
+struct rt_scene {
+  rtgb::DeviceScene d;
+  void* mem = nullptr;
+  size_t bytes = 0;
+  std::vector<RtBVHNode40> nodes40;
+  RtSceneInfo info{};
+  uint32_t max_material = 0;  // largest material index referenced (+1), 0 if none
+  int device = 0;
+};
+
+namespace rtgb {
+
+static thread_local std::string g_error;
+void set_error(const std::string& msg) { g_error = msg; }
+
+static rt_status cuda_fail(cudaError_t e, const char* what) {
+  set_error(std::string(what) + ": " + cudaGetErrorString(e));
+  return RT_ECUDA;
+}
+
+// ---- per-stream workspace ----
+struct Workspace {
+  uint32_t* counters = nullptr;  // 64 words
+  // staging for rt_trace_host
+  void* stage = nullptr;
+  size_t stage_bytes = 0;
+  cudaStream_t copy_in = nullptr, copy_out = nullptr;
+  cudaEvent_t ev[8] = {};
+};
+static std::mutex g_ws_mu;
+static std::map<std::pair<int, cudaStream_t>, Workspace*> g_ws;
+
+static rt_status workspace(cudaStream_t st, Workspace** out) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
+  std::lock_guard<std::mutex> lk(g_ws_mu);
+  auto key = std::make_pair(dev, st);
+  auto it = g_ws.find(key);
+  if (it != g_ws.end()) {
+    *out = it->second;
+    return RT_OK;
+  }
+  Workspace* w = new Workspace();
+  e = cudaMalloc(&w->counters, 64 * sizeof(uint32_t));
+  if (e != cudaSuccess) {
+    delete w;
+    return cuda_fail(e, "cudaMalloc(workspace)");
+  }
+  g_ws[key] = w;
+  *out = w;
+  return RT_OK;
+}
+
+}  // namespace rtgb
+
+using namespace rtgb;
+
+extern "C" {
+
+const char* rt_last_error_string(void) { return g_error.c_str(); }
+uint32_t rt_abi_version(void) { return RT_ABI_VERSION; }
+
+rt_status rt_stream_wait(void* stream, double timeout_seconds) {
+  cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+  const auto t0 = std::chrono::steady_clock::now();
+  for (;;) {
+    cudaError_t e = cudaStreamQuery(st);
+    if (e == cudaSuccess) return RT_OK;
+    if (e != cudaErrorNotReady) return cuda_fail(e, "cudaStreamQuery");
+    const double el = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    if (el >= timeout_seconds) {
+      set_error("rt_stream_wait: deadline passed");
+      return RT_ETIMEOUT;
+    }
+    std::this_thread::sleep_for(std::chrono::microseconds(50));
+  }
+}
+
+rt_status rt_build_bvh(const RtTriangle64* triangles, uint32_t num_triangles, const RtSphere32* spheres,
+                       uint32_t num_spheres, const RtModel64* models, uint32_t num_models, uint32_t bvh_mode,
+                       RtBVHNode40* out_nodes) {
+  const uint64_t N = (uint64_t)num_triangles + num_spheres;
+  if ((num_triangles && !triangles) || (num_spheres && !spheres) || (N && !out_nodes) ||
+      (bvh_mode != RT_BVH_SORTED && bvh_mode != RT_BVH_REFERENCE) || N > kMaxTriangles) {
+    set_error("rt_build_bvh: bad argument");
+    return RT_EINVAL;
+  }
+  std::vector<RtTriangle64> wt;
+  std::vector<RtSphere32> ws;
+  std::string msg;
+  if (!world_space(triangles, num_triangles, spheres, num_spheres, models, num_models, wt, ws, msg)) {
+    set_error("rt_build_bvh: " + msg);
+    return RT_EINVAL;
+  }
+  std::vector<RtBVHNode40> nodes;
+  build_bvh(wt.data(), num_triangles, ws.data(), num_spheres, bvh_mode, nodes);
+  if (!nodes.empty()) std::memcpy(out_nodes, nodes.data(), nodes.size() * sizeof(RtBVHNode40));
+  return RT_OK;
+}
+
+rt_status rt_scene_create_ex(const RtSceneDesc* desc, rt_scene** out_scene) {
+  if (!desc || !out_scene) {
+    set_error("rt_scene_create_ex: null argument");
+    return RT_EINVAL;
+  }
+  *out_scene = nullptr;
+  const uint32_t nt = desc->num_triangles, ns = desc->num_spheres, nm = desc->num_materials;
+  const uint64_t N = (uint64_t)nt + ns;
+  if ((nt && !desc->triangles) || (ns && !desc->spheres) || (nm && !desc->materials)) {
+    set_error("rt_scene_create_ex: null array with non-zero count");
+    return RT_EINVAL;
+  }
+  if (N > kMaxTriangles) {
+    set_error("rt_scene_create_ex: more than 2^27 primitives");
+    return RT_EINVAL;
+  }
+  if (desc->bvh_mode != RT_BVH_SORTED && desc->bvh_mode != RT_BVH_REFERENCE) {
+    set_error("rt_scene_create_ex: unknown bvh_mode");
+    return RT_EINVAL;
+  }
+  if (desc->nodes && N && desc->num_nodes != 2 * N - 1) {
+    set_error("rt_scene_create_ex: num_nodes must be 2*(triangles+spheres)-1");
+    return RT_EINVAL;
+  }
+  const auto t0 = std::chrono::steady_clock::now();
+  std::unique_ptr<rt_scene> sc(new rt_scene());
+  cudaGetDevice(&sc->device);
+  std::vector<RtTriangle64> wt;
+  std::vector<RtSphere32> ws;
+  std::string msg;
+  if (!world_space(desc->triangles, nt, desc->spheres, ns, desc->models, desc->num_models, wt, ws, msg)) {
+    set_error("rt_scene_create_ex: " + msg);
+    return RT_EINVAL;
+  }
+  if (desc->nodes) {
+    sc->nodes40.assign(desc->nodes, desc->nodes + (N ? 2 * N - 1 : 0));
+  } else {
+    build_bvh(wt.data(), nt, ws.data(), ns, desc->bvh_mode, sc->nodes40);
+  }
+  HostDeviceBVH hb;
+  if (!convert_bvh(sc->nodes40.data(), (uint32_t)sc->nodes40.size(), wt.data(), nt, ws.data(), ns, desc->materials, nm,
+                   desc->leaf_size, hb, msg)) {
+    set_error("rt_scene_create_ex: " + msg);
+    return RT_EINVAL;
+  }
+  if (hb.depth >= 127u) {
+    set_error("rt_scene_create_ex: BVH depth " + std::to_string(hb.depth) + " exceeds the 127-level stack");
+    return RT_ESTACK;
+  }
+  uint32_t maxm = 0;
+  for (uint32_t i = 0; i < nt; ++i) maxm = std::max(maxm, wt[i].materialIndex + 1u);
+  for (uint32_t i = 0; i < ns; ++i) maxm = std::max(maxm, ws[i].materialIndex + 1u);
+  sc->max_material = maxm;
+
+  // One device allocation, 256-byte aligned sub-arrays.
+  auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
+  const size_t b_inner = hb.inner.size() * 4, b_tris = hb.tris.size() * 4, b_ids = hb.tri_ids.size() * 4,
+               b_mat = hb.tri_mat.size() * 4, b_sph = hb.spheres.size() * 4, b_mats = hb.mats.size() * 4;
+  const size_t total = al(b_inner) + al(b_tris) + al(b_ids) + al(b_mat) + al(b_sph) + al(b_mats) + 256;
+  cudaError_t e = cudaMalloc(&sc->mem, total);
+  if (e != cudaSuccess) {
+    set_error(std::string("rt_scene_create_ex: cudaMalloc: ") + cudaGetErrorString(e));
+    return RT_ENOMEM;
+  }
+  sc->bytes = total;
+  char* p = static_cast<char*>(sc->mem);
+  auto put = [&](const void* src, size_t bytes) -> const void* {
+    void* dst = p;
+    if (bytes) {
+      cudaError_t ce = cudaMemcpy(dst, src, bytes, cudaMemcpyHostToDevice);
+      if (ce != cudaSuccess) e = ce;
+    }
+    p += al(bytes);
+    return dst;
+  };
+  sc->d.inner = put(hb.inner.data(), b_inner);
+  sc->d.tris = put(hb.tris.data(), b_tris);
+  sc->d.tri_ids = static_cast<const uint32_t*>(put(hb.tri_ids.data(), b_ids));
+  sc->d.tri_mat = static_cast<const uint32_t*>(put(hb.tri_mat.data(), b_mat));
+  sc->d.spheres = put(hb.spheres.data(), b_sph);
+  sc->d.mats = put(hb.mats.data(), b_mats);
+  if (e != cudaSuccess) {
+    cudaFree(sc->mem);
+    sc->mem = nullptr;
+    return cuda_fail(e, "rt_scene_create_ex: upload");
+  }
+  sc->d.root = hb.root;
+  sc->d.n_inner = (uint32_t)(hb.inner.size() / 16);
+  sc->d.n_tris = (uint32_t)hb.tri_ids.size();
+  sc->d.n_spheres = ns;
+  sc->d.n_mats = nm;
+  sc->d.depth = hb.depth;
+  RtSceneInfo& inf = sc->info;
+  inf.num_triangles = nt;
+  inf.num_spheres = ns;
+  inf.num_materials = nm;
+  inf.num_nodes = (uint32_t)sc->nodes40.size();
+  inf.device_nodes = sc->d.n_inner;
+  inf.depth = hb.depth;
+  inf.leaf_size = desc->leaf_size ? desc->leaf_size : kDefaultLeafSize;
+  inf.bvh_mode = desc->bvh_mode;
+  inf.device_bytes = total;
+  inf.build_seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  *out_scene = sc.release();
+  return RT_OK;
+}
+
+rt_status rt_scene_create(const RtTriangle64* triangles, uint32_t num_triangles, const RtSphere32* spheres,
+                          uint32_t num_spheres, const RtMaterial32* materials, uint32_t num_materials,
+                          const RtBVHNode40* nodes, rt_scene** out_scene) {
+  RtSceneDesc d;
+  std::memset(&d, 0, sizeof(d));
+  d.triangles = triangles;
+  d.num_triangles = num_triangles;
+  d.spheres = spheres;
+  d.num_spheres = num_spheres;
+  d.materials = materials;
+  d.num_materials = num_materials;
+  d.nodes = nodes;
+  const uint64_t N = (uint64_t)num_triangles + num_spheres;
+  d.num_nodes = nodes && N ? (uint32_t)(2 * N - 1) : 0;
+  d.bvh_mode = RT_BVH_SORTED;
+  return rt_scene_create_ex(&d, out_scene);
+}
+
+rt_status rt_scene_destroy(rt_scene* scene) {
+  if (!scene) return RT_OK;
+  if (scene->mem) cudaFree(scene->mem);
+  delete scene;
+  return RT_OK;
+}
+
+rt_status rt_scene_get_info(const rt_scene* scene, RtSceneInfo* out_info) {
+  if (!scene || !out_info) {
+    set_error("rt_scene_get_info: null argument");
+    return RT_EINVAL;
+  }
+  *out_info = scene->info;
+  return RT_OK;
+}
+
+rt_status rt_scene_get_nodes(const rt_scene* scene, RtBVHNode40* h_out, uint32_t capacity) {
+  if (!scene || (!h_out && !scene->nodes40.empty())) {
+    set_error("rt_scene_get_nodes: null argument");
+    return RT_EINVAL;
+  }
+  if (capacity < scene->nodes40.size()) {
+    set_error("rt_scene_get_nodes: capacity below num_nodes");
+    return RT_EINVAL;
+  }
+  if (!scene->nodes40.empty())
+    std::memcpy(h_out, scene->nodes40.data(), scene->nodes40.size() * sizeof(RtBVHNode40));
+  return RT_OK;
+}
+
+rt_status rt_trace(rt_scene* scene, const RtRay* d_rays, uint32_t n, RtHit* d_hits, uint32_t flags, void* stream) {
+  if (!scene || (n && (!d_rays || !d_hits)) || flags > RT_TRACE_ANY || n > 0x80000000u) {
+    set_error("rt_trace: bad argument");
+    return RT_EINVAL;
+  }
+  if (n == 0) return RT_OK;
+  cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+  Workspace* w = nullptr;
+  rt_status s = workspace(st, &w);
+  if (s != RT_OK) return s;
+  cudaError_t e = cudaMemsetAsync(w->counters, 0, 2 * sizeof(uint32_t), st);
+  if (e != cudaSuccess) return cuda_fail(e, "rt_trace: memset");
+  e = launch_trace(scene->d, d_rays, n, d_hits, flags, w->counters, stream);
+  if (e != cudaSuccess) return cuda_fail(e, "rt_trace: launch");
+  return RT_OK;
+}
+
+rt_status rt_trace_host(rt_scene* scene, const RtRay* h_rays, uint32_t n, RtHit* h_hits, uint32_t flags,
+                        void* stream) {
+  if (!scene || (n && (!h_rays || !h_hits)) || flags > RT_TRACE_ANY || n > 0x80000000u) {
+    set_error("rt_trace_host: bad argument");
+    return RT_EINVAL;
+  }
+  if (n == 0) return RT_OK;
+  cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+  Workspace* w = nullptr;
+  rt_status s = workspace(st, &w);
+  if (s != RT_OK) return s;
+  // Two buffers of up to `chunk` rays; copy-in, trace and copy-out run on three
+  // streams so chunk i+1 uploads while chunk i traces and chunk i-1 downloads.
+  const uint32_t chunk = std::min<uint32_t>(n, 1u << 21);
+  const uint32_t nchunks = (n + chunk - 1) / chunk;
+  const size_t per = (size_t)chunk * (sizeof(RtRay) + sizeof(RtHit));
+  const size_t need = 2 * per;
+  cudaError_t e;
+  if (w->stage_bytes < need) {
+    if (w->stage) cudaFree(w->stage);
+    w->stage = nullptr;
+    w->stage_bytes = 0;
+    e = cudaMalloc(&w->stage, need);
+    if (e != cudaSuccess) {
+      set_error(std::string("rt_trace_host: staging cudaMalloc: ") + cudaGetErrorString(e));
+      return RT_ENOMEM;
+    }
+    w->stage_bytes = need;
+  }
+  if (!w->copy_in) {
+    if ((e = cudaStreamCreateWithFlags(&w->copy_in, cudaStreamNonBlocking)) != cudaSuccess) return cuda_fail(e, "stream");
+    if ((e = cudaStreamCreateWithFlags(&w->copy_out, cudaStreamNonBlocking)) != cudaSuccess) return cuda_fail(e, "stream");
+    for (auto& ev : w->ev)
+      if ((e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming)) != cudaSuccess) return cuda_fail(e, "event");
+  }
+  char* base = static_cast<char*>(w->stage);
+  RtRay* drays[2] = {reinterpret_cast<RtRay*>(base), reinterpret_cast<RtRay*>(base + per)};
+  RtHit* dhits[2] = {reinterpret_cast<RtHit*>(base + (size_t)chunk * sizeof(RtRay)),
+                     reinterpret_cast<RtHit*>(base + per + (size_t)chunk * sizeof(RtRay))};
+  cudaEvent_t* in_done = &w->ev[0];
+  cudaEvent_t* trace_done = &w->ev[2];
+  cudaEvent_t* out_done = &w->ev[4];
+  // the caller's earlier work on `stream` comes first
+  if ((e = cudaEventRecord(w->ev[6], st)) != cudaSuccess) return cuda_fail(e, "event");
+  if ((e = cudaStreamWaitEvent(w->copy_in, w->ev[6], 0)) != cudaSuccess) return cuda_fail(e, "wait");
+  for (uint32_t c = 0; c < nchunks; ++c) {
+    const uint32_t b = c & 1u;
+    const uint32_t off = c * chunk;
+    const uint32_t cnt = std::min(chunk, n - off);
+    if (c >= 2 && (e = cudaStreamWaitEvent(w->copy_in, out_done[b], 0)) != cudaSuccess) return cuda_fail(e, "wait");
+    if ((e = cudaMemcpyAsync(drays[b], h_rays + off, (size_t)cnt * sizeof(RtRay), cudaMemcpyHostToDevice,
+                             w->copy_in)) != cudaSuccess)
+      return cuda_fail(e, "rt_trace_host: H2D");
+    if ((e = cudaEventRecord(in_done[b], w->copy_in)) != cudaSuccess) return cuda_fail(e, "event");
+    if ((e = cudaStreamWaitEvent(st, in_done[b], 0)) != cudaSuccess) return cuda_fail(e, "wait");
+    if ((e = cudaMemsetAsync(w->counters, 0, 2 * sizeof(uint32_t), st)) != cudaSuccess) return cuda_fail(e, "memset");
+    if ((e = launch_trace(scene->d, drays[b], cnt, dhits[b], flags, w->counters, stream)) != cudaSuccess)
+      return cuda_fail(e, "rt_trace_host: launch");
+    if ((e = cudaEventRecord(trace_done[b], st)) != cudaSuccess) return cuda_fail(e, "event");
+    if ((e = cudaStreamWaitEvent(w->copy_out, trace_done[b], 0)) != cudaSuccess) return cuda_fail(e, "wait");
+    if ((e = cudaMemcpyAsync(h_hits + off, dhits[b], (size_t)cnt * sizeof(RtHit), cudaMemcpyDeviceToHost,
+                             w->copy_out)) != cudaSuccess)
+      return cuda_fail(e, "rt_trace_host: D2H");
+    if ((e = cudaEventRecord(out_done[b], w->copy_out)) != cudaSuccess) return cuda_fail(e, "event");
+  }
+  // the caller's stream continues after the last download
+  if ((e = cudaEventRecord(w->ev[7], w->copy_out)) != cudaSuccess) return cuda_fail(e, "event");
+  if ((e = cudaStreamWaitEvent(st, w->ev[7], 0)) != cudaSuccess) return cuda_fail(e, "wait");
+  if ((e = cudaStreamSynchronize(w->copy_out)) != cudaSuccess) return cuda_fail(e, "rt_trace_host: sync");
+  return RT_OK;
+}
+
+rt_status rt_render(rt_scene* scene, const RtRaytraceUBO* ubo, float* d_accum, uint32_t width, uint32_t height,
+                    uint32_t spp, const RtRenderOptions* opt, void* stream) {
+  if (!scene || !ubo || !d_accum || width == 0 || height == 0 || (uint64_t)width * height > 0x40000000ull) {
+    set_error("rt_render: bad argument");
+    return RT_EINVAL;
+  }
+  if (scene->max_material > scene->d.n_mats) {
+    set_error("rt_render: a primitive names a material index >= num_materials");
+    return RT_EINVAL;
+  }
+  RtRenderOptions o;
+  std::memset(&o, 0, sizeof(o));
+  if (opt) o = *opt;
+  if (o.shade_mode != RT_SHADE_REFERENCE && o.shade_mode != RT_SHADE_EXTENDED) {
+    set_error("rt_render: unknown shade_mode");
+    return RT_EINVAL;
+  }
+  if (spp == 0) return RT_OK;
+  cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+  Workspace* w = nullptr;
+  rt_status s = workspace(st, &w);
+  if (s != RT_OK) return s;
+  float cam[12];
+  camera_setup(*ubo, width, height, cam);
+  cudaError_t e = cudaMemsetAsync(w->counters, 0, 2 * sizeof(uint32_t), st);
+  if (e != cudaSuccess) return cuda_fail(e, "rt_render: memset");
+  e = launch_render(scene->d, cam, ubo->maxRayTraceDepth, ubo->randomState, d_accum, width, height, spp, o.shade_mode,
+                    o.background, w->counters, stream);
+  if (e != cudaSuccess) return cuda_fail(e, "rt_render: launch");
+  return RT_OK;
+}
+
+rt_status rt_accum_clear(float* d_accum, uint32_t width, uint32_t height, void* stream) {
+  if (!d_accum || (uint64_t)width * height > 0x40000000ull) {
+    set_error("rt_accum_clear: bad argument");
+    return RT_EINVAL;
+  }
+  cudaError_t e = launch_accum_clear(d_accum, width, height, stream);
+  return e == cudaSuccess ? RT_OK : cuda_fail(e, "rt_accum_clear");
+}
+
+rt_status rt_resolve(const float* d_accum, uint32_t width, uint32_t height, uint32_t spp, float* d_out, void* stream) {
+  if (!d_accum || !d_out || spp == 0 || (uint64_t)width * height > 0x40000000ull) {
+    set_error("rt_resolve: bad argument");
+    return RT_EINVAL;
+  }
+  cudaError_t e = launch_resolve(d_accum, width, height, spp, d_out, stream);
+  return e == cudaSuccess ? RT_OK : cuda_fail(e, "rt_resolve");
+}
+
+}  // extern "C"

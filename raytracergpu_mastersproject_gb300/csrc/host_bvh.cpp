@@ -1,0 +1,554 @@
+// host_bvh.cpp -- host BVH build in the reference node layout, and its
+// conversion to the device form.
+//
+// The build reproduces the six S1 compute passes of the reference
+// (RaytracerBVH.cpp:778-991) on the host, multi-threaded:
+//   ModelSpaceToWorldSpace.comp:32-48          world_space()
+//   GetEnclosingAABB.comp:64-109               centroid box, padded
+//   GenerateMortonCodesOfPrimitives.comp:52-93 30-bit codes
+//   RadixSortSimple.comp:59-157                stable LSD sort, 4 x 8 bits
+//   ConstructHLBVH.comp:145-214                Karras internal nodes + leaves
+//   ConstructAABBsOfInternalNodes.comp:38-64   bottom-up box union
+// Mode RT_BVH_REFERENCE keeps the reference's two quirks: Morton quantisation
+// of coord/span instead of (coord-min)/span (:60-65), and leaf slot k holding
+// primitive k rather than the k-th sorted primitive (ConstructHLBVH.comp:152-169).
+// Mode RT_BVH_SORTED corrects both; its node array has the same layout.
+//
+// This translation unit is compiled with -ffp-contract=off: every binary32
+// operation is rounded on its own, in the order written, as the shaders state.
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstdlib>
+#include <cstring>
+#include <thread>
+
+#include "rt_internal.h"
+
+namespace rtgb {
+
+unsigned host_threads() {
+  static unsigned cached = [] {
+    unsigned n = std::thread::hardware_concurrency();
+    if (const char* e = std::getenv("RT_HOST_THREADS")) {
+      long v = std::strtol(e, nullptr, 10);
+      if (v > 0) n = (unsigned)v;
+    }
+    if (n == 0) n = 1;
+    if (n > 128) n = 128;
+    return n;
+  }();
+  return cached;
+}
+
+static inline uint32_t f2u_sat(float f) {
+  if (!(f > 0.0f)) return 0u;
+  if (f >= 4294967296.0f) return 0xFFFFFFFFu;
+  return (uint32_t)f;
+}
+
+// GenerateMortonCodesOfPrimitives.comp:41-50
+static inline uint32_t spread3(uint32_t v) {
+  if (v == 1024u) v--;
+  v = (v | (v << 16)) & 0x030000FFu;
+  v = (v | (v << 8)) & 0x0300F00Fu;
+  v = (v | (v << 4)) & 0x030C30C3u;
+  v = (v | (v << 2)) & 0x09249249u;
+  return v;
+}
+
+static inline void pad_axis(float& mn, float& mx) {
+  const float delta = 0.001f, padding = delta / 2.0f;  // ConstructHLBVH.comp:38-39
+  if (mx - mn < delta) {
+    mn -= padding;
+    mx += padding;
+  }
+}
+
+bool world_space(const RtTriangle64* tris, uint32_t nt, const RtSphere32* sph, uint32_t ns,
+                 const RtModel64* models, uint32_t nm, std::vector<RtTriangle64>& out_t,
+                 std::vector<RtSphere32>& out_s, std::string& msg) {
+  out_t.assign(tris, tris + nt);
+  out_s.assign(sph, sph + ns);
+  if (!models) return true;
+  for (uint32_t i = 0; i < nt; ++i)
+    if (tris[i].modelIndex >= nm) {
+      msg = "triangle " + std::to_string(i) + " has modelIndex out of range";
+      return false;
+    }
+  for (uint32_t i = 0; i < ns; ++i)
+    if (sph[i].modelIndex >= nm) {
+      msg = "sphere " + std::to_string(i) + " has modelIndex out of range";
+      return false;
+    }
+  // ModelSpaceToWorldSpace.comp:37-45: v' = M * vec4(v.xyz, 1), column-major M.
+  auto xform = [](const float* m, float* v) {
+    float x = v[0], y = v[1], z = v[2], w = 1.0f;
+    float r[4];
+    for (int row = 0; row < 4; ++row) r[row] = m[0 + row] * x + m[4 + row] * y + m[8 + row] * z + m[12 + row] * w;
+    std::memcpy(v, r, sizeof(r));
+  };
+  parallel_for(nt, [&](size_t b, size_t e, unsigned) {
+    for (size_t i = b; i < e; ++i) {
+      const float* m = models[out_t[i].modelIndex].m;
+      xform(m, out_t[i].v0);
+      xform(m, out_t[i].v1);
+      xform(m, out_t[i].v2);
+    }
+  });
+  for (uint32_t i = 0; i < ns; ++i) xform(models[out_s[i].modelIndex].m, out_s[i].center);
+  return true;
+}
+
+// Stable LSD radix sort of (key, value) by key, 4 passes of 8 bits
+// (the bin width of RadixSortSimple.comp:8-13), parallel over chunks with
+// per-chunk histograms so that equal keys keep their input order.
+static void radix_sort_pairs(std::vector<uint32_t>& keys, std::vector<uint32_t>& vals) {
+  size_t n = keys.size();
+  std::vector<uint32_t> k2(n), v2(n);
+  unsigned T = std::min<unsigned>(host_threads(), (unsigned)std::max<size_t>(1, n / 65536));
+  if (T == 0) T = 1;
+  size_t per = (n + T - 1) / T;
+  std::vector<uint32_t> hist((size_t)T * 256);
+  for (int pass = 0; pass < 4; ++pass) {
+    uint32_t shift = 8u * (uint32_t)pass;
+    std::fill(hist.begin(), hist.end(), 0u);
+    auto count = [&](unsigned t) {
+      size_t b = t * per, e = std::min(n, b + per);
+      uint32_t* h = &hist[(size_t)t * 256];
+      for (size_t i = b; i < e; ++i) h[(keys[i] >> shift) & 255u]++;
+    };
+    std::vector<std::thread> th;
+    for (unsigned t = 1; t < T; ++t) th.emplace_back(count, t);
+    count(0);
+    for (auto& x : th) x.join();
+    th.clear();
+    uint32_t acc = 0;
+    for (int bin = 0; bin < 256; ++bin)
+      for (unsigned t = 0; t < T; ++t) {
+        uint32_t c = hist[(size_t)t * 256 + bin];
+        hist[(size_t)t * 256 + bin] = acc;
+        acc += c;
+      }
+    auto scatter = [&](unsigned t) {
+      size_t b = t * per, e = std::min(n, b + per);
+      uint32_t* h = &hist[(size_t)t * 256];
+      for (size_t i = b; i < e; ++i) {
+        uint32_t dst = h[(keys[i] >> shift) & 255u]++;
+        k2[dst] = keys[i];
+        v2[dst] = vals[i];
+      }
+    };
+    for (unsigned t = 1; t < T; ++t) th.emplace_back(scatter, t);
+    scatter(0);
+    for (auto& x : th) x.join();
+    keys.swap(k2);
+    vals.swap(v2);
+  }
+}
+
+// ConstructHLBVH.comp:58-70
+static inline int delta(const uint32_t* codes, int n, int i, int j) {
+  if (j < 0 || j > n - 1) return -1;
+  uint32_t ci = codes[i], cj = codes[j];
+  if (ci == cj) return 32 + __builtin_clz((uint32_t)i ^ (uint32_t)j);
+  return __builtin_clz(ci ^ cj);
+}
+
+void build_bvh(const RtTriangle64* tris, uint32_t nt, const RtSphere32* sph, uint32_t ns, uint32_t mode,
+               std::vector<RtBVHNode40>& nodes) {
+  const uint32_t N = nt + ns;
+  nodes.clear();
+  if (N == 0) return;
+  nodes.resize(2 * (size_t)N - 1);
+
+  // Centroids (GetEnclosingAABB.comp:40-42): ((v0 + v1 + v2) / 3).xyz
+  std::vector<float> cen(3 * (size_t)N);
+  parallel_for(N, [&](size_t b, size_t e, unsigned) {
+    for (size_t i = b; i < e; ++i) {
+      if (i < nt) {
+        const RtTriangle64& t = tris[i];
+        for (int k = 0; k < 3; ++k) cen[3 * i + k] = (t.v0[k] + t.v1[k] + t.v2[k]) / 3.0f;
+      } else {
+        const RtSphere32& s = sph[i - nt];
+        for (int k = 0; k < 3; ++k) cen[3 * i + k] = s.center[k];
+      }
+    }
+  });
+
+  // Enclosing box of the centroids, preset to +-1e9 (GetEnclosingAABB.comp:72-76),
+  // then padded (:105-109).
+  unsigned T = host_threads();
+  std::vector<float> part(6 * (size_t)T);
+  for (unsigned t = 0; t < T; ++t)
+    for (int k = 0; k < 3; ++k) {
+      part[6 * t + k] = 1000000000.0f;
+      part[6 * t + 3 + k] = -1000000000.0f;
+    }
+  parallel_for(N, [&](size_t b, size_t e, unsigned t) {
+    float* p = &part[6 * (size_t)t];
+    for (size_t i = b; i < e; ++i)
+      for (int k = 0; k < 3; ++k) {
+        p[k] = std::fmin(p[k], cen[3 * i + k]);
+        p[3 + k] = std::fmax(p[3 + k], cen[3 * i + k]);
+      }
+  });
+  float emin[3], emax[3];
+  for (int k = 0; k < 3; ++k) {
+    emin[k] = 1000000000.0f;
+    emax[k] = -1000000000.0f;
+    for (unsigned t = 0; t < T; ++t) {
+      emin[k] = std::fmin(emin[k], part[6 * t + k]);
+      emax[k] = std::fmax(emax[k], part[6 * t + 3 + k]);
+    }
+    pad_axis(emin[k], emax[k]);
+  }
+
+  // Morton codes (GenerateMortonCodesOfPrimitives.comp:60-65, 88-90).
+  std::vector<uint32_t> codes(N), order(N);
+  parallel_for(N, [&](size_t b, size_t e, unsigned) {
+    for (size_t i = b; i < e; ++i) {
+      uint32_t q[3];
+      for (int k = 0; k < 3; ++k) {
+        float span = emax[k] - emin[k];
+        float off = mode == RT_BVH_REFERENCE ? cen[3 * i + k] / span : (cen[3 * i + k] - emin[k]) / span;
+        q[k] = f2u_sat(off * 1024.0f);
+      }
+      codes[i] = (spread3(q[2]) << 2) | (spread3(q[1]) << 1) | spread3(q[0]);
+      order[i] = (uint32_t)i;
+    }
+  });
+  radix_sort_pairs(codes, order);
+
+  // Leaves (ConstructHLBVH.comp:151-169), padded boxes (:41-54, 117-143).
+  const uint32_t leaf_off = N - 1;
+  parallel_for(N, [&](size_t b, size_t e, unsigned) {
+    for (size_t k = b; k < e; ++k) {
+      uint32_t g = mode == RT_BVH_REFERENCE ? (uint32_t)k : order[k];
+      RtBVHNode40& nd = nodes[leaf_off + k];
+      if (g < nt) {
+        const RtTriangle64& t = tris[g];
+        nd.minX = std::fmin(t.v0[0], std::fmin(t.v1[0], t.v2[0]));
+        nd.maxX = std::fmax(t.v0[0], std::fmax(t.v1[0], t.v2[0]));
+        nd.minY = std::fmin(t.v0[1], std::fmin(t.v1[1], t.v2[1]));
+        nd.maxY = std::fmax(t.v0[1], std::fmax(t.v1[1], t.v2[1]));
+        nd.minZ = std::fmin(t.v0[2], std::fmin(t.v1[2], t.v2[2]));
+        nd.maxZ = std::fmax(t.v0[2], std::fmax(t.v1[2], t.v2[2]));
+        nd.primitiveIndex = g;
+        nd.primitiveType = RT_PRIM_TRIANGLE;
+      } else {
+        const RtSphere32& s = sph[g - nt];
+        float l[3], r[3];
+        for (int a = 0; a < 3; ++a) {
+          l[a] = s.center[a] - s.radius;
+          r[a] = s.center[a] + s.radius;
+        }
+        nd.minX = std::fmin(l[0], r[0]);
+        nd.maxX = std::fmax(l[0], r[0]);
+        nd.minY = std::fmin(l[1], r[1]);
+        nd.maxY = std::fmax(l[1], r[1]);
+        nd.minZ = std::fmin(l[2], r[2]);
+        nd.maxZ = std::fmax(l[2], r[2]);
+        nd.primitiveIndex = g - nt;
+        nd.primitiveType = RT_PRIM_SPHERE;
+      }
+      pad_axis(nd.minX, nd.maxX);
+      pad_axis(nd.minY, nd.maxY);
+      pad_axis(nd.minZ, nd.maxZ);
+      nd.left = 0;
+      nd.right = 0;
+    }
+  });
+
+  // Internal nodes: Karras range + split (ConstructHLBVH.comp:72-115, 171-209).
+  std::vector<uint32_t> parent(2 * (size_t)N - 1, 0u);
+  const uint32_t* C = codes.data();
+  const int n = (int)N;
+  parallel_for(N > 0 ? N - 1 : 0, [&](size_t b, size_t e, unsigned) {
+    for (size_t ii = b; ii < e; ++ii) {
+      int id = (int)ii;
+      int dl = delta(C, n, id, id - 1), dr = delta(C, n, id, id + 1);
+      int dir = dr >= dl ? 1 : -1;
+      int dmin = std::min(dl, dr);
+      int lmax = 2;
+      while (delta(C, n, id, id + lmax * dir) > dmin) lmax <<= 1;
+      int l = 0;
+      for (int t = lmax >> 1; t > 0; t >>= 1)
+        if (delta(C, n, id, id + (l + t) * dir) > dmin) l += t;
+      int end = id + l * dir;
+      int first = std::min(id, end), last = std::max(id, end);
+      int common = delta(C, n, first, last);
+      int split = first, stride = last - first;
+      do {
+        stride = (stride + 1) >> 1;
+        int ns2 = split + stride;
+        if (ns2 < last && delta(C, n, first, ns2) > common) split = ns2;
+      } while (stride > 1);
+      uint32_t lc = (uint32_t)(split == first ? (int)leaf_off + split : split);
+      uint32_t rc = (uint32_t)(split + 1 == last ? (int)leaf_off + split + 1 : split + 1);
+      RtBVHNode40& nd = nodes[ii];
+      nd.minX = nd.maxX = nd.minY = nd.maxY = nd.minZ = nd.maxZ = 0.0f;
+      nd.left = lc;
+      nd.right = rc;
+      nd.primitiveIndex = 0;
+      nd.primitiveType = 0;
+      parent[lc] = (uint32_t)ii;
+      parent[rc] = (uint32_t)ii;
+    }
+  });
+  if (N == 1) return;
+
+  // Bottom-up boxes (ConstructAABBsOfInternalNodes.comp:38-64): the second
+  // child to arrive at a node forms the union and continues upward.
+  std::vector<std::atomic<int>> visits(N - 1);
+  for (auto& v : visits) v.store(0, std::memory_order_relaxed);
+  parallel_for(N, [&](size_t b, size_t e, unsigned) {
+    for (size_t i = b; i < e; ++i) {
+      uint32_t node = parent[leaf_off + i];
+      for (;;) {
+        int v = visits[node].fetch_add(1, std::memory_order_acq_rel);
+        if (v < 1) break;
+        RtBVHNode40& nd = nodes[node];
+        const RtBVHNode40& L = nodes[nd.left];
+        const RtBVHNode40& R = nodes[nd.right];
+        nd.minX = std::fmin(L.minX, R.minX);
+        nd.maxX = std::fmax(L.maxX, R.maxX);
+        nd.minY = std::fmin(L.minY, R.minY);
+        nd.maxY = std::fmax(L.maxY, R.maxY);
+        nd.minZ = std::fmin(L.minZ, R.minZ);
+        nd.maxZ = std::fmax(L.maxZ, R.maxZ);
+        std::atomic_thread_fence(std::memory_order_release);
+        if (node == 0) break;
+        node = parent[node];
+      }
+    }
+  });
+}
+
+// triangleHit's vertex-only values (raytraceBVH.comp:119-125), binary32.
+static void precompute_triangle(const RtTriangle64& T, float* r) {
+  float v0x = T.v0[0], v0y = T.v0[1], v0z = T.v0[2];
+  float ux = T.v1[0] - v0x, uy = T.v1[1] - v0y, uz = T.v1[2] - v0z;
+  float vx = T.v2[0] - v0x, vy = T.v2[1] - v0y, vz = T.v2[2] - v0z;
+  float Nx = uy * vz - uz * vy, Ny = uz * vx - ux * vz, Nz = ux * vy - uy * vx;
+  float nn = Nx * Nx + Ny * Ny + Nz * Nz;
+  float len = std::sqrt(nn);
+  float nx = Nx / len, ny = Ny / len, nz = Nz / len;
+  float D = nx * v0x + ny * v0y + nz * v0z;
+  float wx = Nx / nn, wy = Ny / nn, wz = Nz / nn;
+  float vals[16] = {nx, ny, nz, D, wx, wy, wz, v0x, v0y, v0z, ux, uy, uz, vx, vy, vz};
+  std::memcpy(r, vals, sizeof(vals));
+}
+
+static inline float bits_f(uint32_t u) {
+  float f;
+  std::memcpy(&f, &u, 4);
+  return f;
+}
+
+bool convert_bvh(const RtBVHNode40* nodes, uint32_t nn, const RtTriangle64* tris, uint32_t nt,
+                 const RtSphere32* sph, uint32_t ns, const RtMaterial32* mats, uint32_t nm,
+                 uint32_t leaf_size, HostDeviceBVH& out, std::string& msg) {
+  out = HostDeviceBVH();
+  if (leaf_size == 0) leaf_size = kDefaultLeafSize;
+  if (leaf_size > kMaxLeafSize) {
+    msg = "leaf_size above " + std::to_string(kMaxLeafSize);
+    return false;
+  }
+  // spheres and materials in caller order
+  out.spheres.resize(8 * (size_t)ns);
+  for (uint32_t i = 0; i < ns; ++i) {
+    float* s = &out.spheres[8 * (size_t)i];
+    s[0] = sph[i].center[0]; s[1] = sph[i].center[1]; s[2] = sph[i].center[2]; s[3] = sph[i].radius;
+    s[4] = bits_f(sph[i].materialIndex); s[5] = 0.0f; s[6] = 0.0f; s[7] = 0.0f;
+  }
+  out.mats.resize(8 * (size_t)nm);
+  for (uint32_t i = 0; i < nm; ++i) {
+    float* m = &out.mats[8 * (size_t)i];
+    m[0] = mats[i].albedo[0]; m[1] = mats[i].albedo[1]; m[2] = mats[i].albedo[2]; m[3] = 0.0f;
+    m[4] = bits_f(mats[i].materialType); m[5] = mats[i].fuzz; m[6] = mats[i].ior; m[7] = 0.0f;
+  }
+  if (nn == 0) return true;
+
+  // Pass A: left-first DFS from node 0; triangle leaves get slots in visit order.
+  const uint32_t NONE = 0xFFFFFFFFu;
+  std::vector<uint32_t> pre;
+  pre.reserve(nn);
+  std::vector<uint8_t> seen(nn, 0);
+  std::vector<uint32_t> slot(nn, NONE);
+  std::vector<uint32_t> stack;
+  stack.push_back(0);
+  while (!stack.empty()) {
+    uint32_t x = stack.back();
+    stack.pop_back();
+    if (x >= nn) {
+      msg = "node index " + std::to_string(x) + " out of range";
+      return false;
+    }
+    if (seen[x]) {
+      msg = "node " + std::to_string(x) + " reached twice: not a tree";
+      return false;
+    }
+    seen[x] = 1;
+    pre.push_back(x);
+    const RtBVHNode40& nd = nodes[x];
+    if (nd.left == 0u && nd.right == 0u) {
+      if (nd.primitiveType == RT_PRIM_TRIANGLE) {
+        if (nd.primitiveIndex >= nt) {
+          msg = "leaf " + std::to_string(x) + " names triangle out of range";
+          return false;
+        }
+        slot[x] = (uint32_t)out.tri_ids.size();
+        out.tri_ids.push_back(nd.primitiveIndex);
+      } else if (nd.primitiveType == RT_PRIM_SPHERE) {
+        if (nd.primitiveIndex >= ns) {
+          msg = "leaf " + std::to_string(x) + " names sphere out of range";
+          return false;
+        }
+      }
+    } else {
+      stack.push_back(nd.right);
+      stack.push_back(nd.left);
+    }
+  }
+  const uint32_t nslots = (uint32_t)out.tri_ids.size();
+  if (nslots > kMaxTriangles) {
+    msg = "more than 2^27 triangle leaves";
+    return false;
+  }
+
+  // Pass B: subtree triangle counts, sphere presence, first slot.
+  std::vector<uint32_t> cnt(nn, 0), first(nn, NONE);
+  std::vector<uint8_t> has_sph(nn, 0), other(nn, 0);
+  for (size_t k = pre.size(); k-- > 0;) {
+    uint32_t x = pre[k];
+    const RtBVHNode40& nd = nodes[x];
+    if (nd.left == 0u && nd.right == 0u) {
+      if (nd.primitiveType == RT_PRIM_TRIANGLE) {
+        cnt[x] = 1;
+        first[x] = slot[x];
+      } else if (nd.primitiveType == RT_PRIM_SPHERE) {
+        has_sph[x] = 1;
+      } else {
+        other[x] = 1;
+      }
+    } else {
+      cnt[x] = cnt[nd.left] + cnt[nd.right];
+      has_sph[x] = has_sph[nd.left] | has_sph[nd.right];
+      other[x] = other[nd.left] | other[nd.right];
+      first[x] = first[nd.left] != NONE ? first[nd.left] : first[nd.right];
+    }
+  }
+  auto is_leaf = [&](uint32_t x) { return nodes[x].left == 0u && nodes[x].right == 0u; };
+  auto collapsible = [&](uint32_t x) {
+    return !is_leaf(x) && cnt[x] >= 1 && cnt[x] <= leaf_size && !has_sph[x] && !other[x];
+  };
+  const uint32_t EMPTY = kLeafBit | kSphereBit | kSphereMask;
+  auto leaf_ref = [&](uint32_t x) -> uint32_t {
+    const RtBVHNode40& nd = nodes[x];
+    if (nd.primitiveType == RT_PRIM_TRIANGLE) return kLeafBit | slot[x];
+    if (nd.primitiveType == RT_PRIM_SPHERE) return kLeafBit | kSphereBit | nd.primitiveIndex;
+    return EMPTY;
+  };
+
+  // Pass C: device indices, preorder over the kept internal nodes.
+  std::vector<uint32_t> dev(nn, NONE);
+  std::vector<uint32_t> kept;
+  std::vector<std::pair<uint32_t, uint32_t>> st2;  // (node, depth)
+  uint32_t maxdepth = 0;
+  auto ref_of = [&](uint32_t x) -> uint32_t {
+    if (is_leaf(x)) return leaf_ref(x);
+    if (collapsible(x)) return kLeafBit | ((cnt[x] - 1u) << kCountShift) | first[x];
+    return dev[x];
+  };
+  if (is_leaf(0) || collapsible(0)) {
+    out.root = ref_of(0);
+    out.depth = 0;
+  } else {
+    st2.push_back({0u, 1u});
+    while (!st2.empty()) {
+      auto [x, d] = st2.back();
+      st2.pop_back();
+      dev[x] = (uint32_t)kept.size();
+      kept.push_back(x);
+      maxdepth = std::max(maxdepth, d);
+      const RtBVHNode40& nd = nodes[x];
+      if (!is_leaf(nd.right) && !collapsible(nd.right)) st2.push_back({nd.right, d + 1});
+      if (!is_leaf(nd.left) && !collapsible(nd.left)) st2.push_back({nd.left, d + 1});
+    }
+    out.root = 0;
+    out.depth = maxdepth;
+  }
+
+  // Pass D: device nodes.
+  out.inner.resize(16 * kept.size());
+  parallel_for(kept.size(), [&](size_t b, size_t e, unsigned) {
+    for (size_t i = b; i < e; ++i) {
+      const RtBVHNode40& nd = nodes[kept[i]];
+      const RtBVHNode40& L = nodes[nd.left];
+      const RtBVHNode40& R = nodes[nd.right];
+      float* o = &out.inner[16 * i];
+      o[0] = L.minX; o[1] = L.maxX; o[2] = L.minY; o[3] = L.maxY;
+      o[4] = R.minX; o[5] = R.maxX; o[6] = R.minY; o[7] = R.maxY;
+      o[8] = L.minZ; o[9] = L.maxZ; o[10] = R.minZ; o[11] = R.maxZ;
+      o[12] = bits_f(ref_of(nd.left));
+      o[13] = bits_f(ref_of(nd.right));
+      o[14] = 0.0f;
+      o[15] = 0.0f;
+    }
+  });
+
+  // Triangle records in slot order.
+  out.tris.resize(16 * (size_t)nslots);
+  out.tri_mat.resize(nslots);
+  parallel_for(nslots, [&](size_t b, size_t e, unsigned) {
+    for (size_t s = b; s < e; ++s) {
+      const RtTriangle64& T = tris[out.tri_ids[s]];
+      precompute_triangle(T, &out.tris[16 * s]);
+      out.tri_mat[s] = T.materialIndex;
+    }
+  });
+  return true;
+}
+
+// raytraceBVH.comp:54-76 evaluated once per frame.
+void camera_setup(const RtRaytraceUBO& ubo, uint32_t width, uint32_t height, float out[12]) {
+  auto normalize3 = [](float* v) {
+    float l = std::sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]);
+    v[0] = v[0] / l; v[1] = v[1] / l; v[2] = v[2] / l;
+  };
+  auto cross3 = [](const float* a, const float* b, float* r) {
+    r[0] = a[1] * b[2] - a[2] * b[1];
+    r[1] = a[2] * b[0] - a[0] * b[2];
+    r[2] = a[0] * b[1] - a[1] * b[0];
+  };
+  float W = (float)width, H = (float)height;
+  float aspect = W / H;
+  float theta = ubo.verticalFOV * 0x1.1df46ap-6f;  // radians()
+  float h = (float)std::tan((double)(theta / 2.0f));
+  float vh = 2.0f * h * 10.0f;                      // _FOCAL_DISTANCE = 10
+  float vw = vh * aspect;
+  float w[3] = {ubo.camPos[0] - ubo.camLookAt[0], ubo.camPos[1] - ubo.camLookAt[1], ubo.camPos[2] - ubo.camLookAt[2]};
+  normalize3(w);
+  float u[3];
+  cross3(ubo.camUpDir, w, u);
+  normalize3(u);
+  float v[3];
+  cross3(w, u, v);
+  float vpu[3], vpv[3], pdu[3], pdv[3], p00[3];
+  for (int k = 0; k < 3; ++k) {
+    vpu[k] = u[k] * vw;
+    vpv[k] = -v[k] * vh;
+    pdu[k] = vpu[k] / W;
+    pdv[k] = vpv[k] / H;
+  }
+  for (int k = 0; k < 3; ++k) {
+    float ul = ((ubo.camPos[k] - w[k] * 10.0f) - vpu[k] / 2.0f) - vpv[k] / 2.0f;
+    p00[k] = ul + (pdu[k] + pdv[k]) * 0.5f;
+  }
+  float vals[12] = {ubo.camPos[0], ubo.camPos[1], ubo.camPos[2], p00[0], p00[1], p00[2],
+                    pdu[0], pdu[1], pdu[2], pdv[0], pdv[1], pdv[2]};
+  std::memcpy(out, vals, sizeof(vals));
+}
+
+}  // namespace rtgb

@@ -1,0 +1,134 @@
+// rt_internal.h -- internal types shared by the host C++ and the CUDA sources.
+//
+// Device form of a scene (all arrays in HBM, read through the non-coherent path):
+//
+//   inner   : one 64-byte record per internal node of the binary BVH; the node
+//             stores the boxes of its two children, so one fetch decides which
+//             children a ray enters and in which order.
+//               float4 a = (c0.lo.x, c0.hi.x, c0.lo.y, c0.hi.y)
+//               float4 b = (c1.lo.x, c1.hi.x, c1.lo.y, c1.hi.y)
+//               float4 c = (c0.lo.z, c0.hi.z, c1.lo.z, c1.hi.z)
+//               uint4  d = (ref0, ref1, 0, 0)
+//   tris    : one 64-byte record per triangle, in BVH leaf order, holding the
+//             values triangleHit (raytraceBVH.comp:118-149) derives from the
+//             vertices, computed once with the same binary32 operations:
+//               float4 (n.x, n.y, n.z, D)   n = normalize(cross(u,v)), D = dot(n,v0)
+//               float4 (w.x, w.y, w.z, v0.x) w = N / dot(N,N)
+//               float4 (v0.y, v0.z, u.x, u.y)
+//               float4 (u.z, v.x, v.y, v.z)
+//   tri_ids : leaf slot -> caller's triangle index
+//   tri_mat : leaf slot -> material index
+//   spheres : 32 B each, caller order: float4 (c.xyz, r), uint4 (material, ...)
+//   mats    : 32 B each: float4 albedo, float4 (type bits, fuzz, ior, 0)
+//
+// A child reference ("ref") is a uint32:
+//   bit31 = 0            internal node index
+//   bit31 = 1, bit30 = 0 triangle leaf: bits 27..29 = count-1, bits 0..26 = first slot
+//   bit31 = 1, bit30 = 1 sphere leaf: bits 0..29 = sphere index
+#pragma once
+
+#include <algorithm>
+#include <cstddef>
+#include <cstdint>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "../../include/rt_gb300.h"
+
+namespace rtgb {
+
+constexpr uint32_t kLeafBit = 0x80000000u;
+constexpr uint32_t kSphereBit = 0x40000000u;
+constexpr uint32_t kCountShift = 27;
+constexpr uint32_t kSlotMask = (1u << 27) - 1u;
+constexpr uint32_t kSphereMask = (1u << 30) - 1u;
+constexpr uint32_t kMaxLeafSize = 8;
+constexpr uint32_t kMaxTriangles = 1u << 27;
+constexpr uint32_t kSentinel = 0x7FFFFFFFu;  // stack bottom, never a node index
+constexpr uint32_t kDefaultLeafSize = 1;
+
+struct DeviceScene {
+  const void* inner = nullptr;     // float4[4 * n_inner]
+  const void* tris = nullptr;      // float4[4 * n_tris]
+  const uint32_t* tri_ids = nullptr;
+  const uint32_t* tri_mat = nullptr;
+  const void* spheres = nullptr;   // float4[2 * n_spheres]
+  const void* mats = nullptr;      // float4[2 * n_mats]
+  uint32_t root = kSentinel;       // ref of the root (kSentinel: empty scene)
+  uint32_t n_inner = 0;
+  uint32_t n_tris = 0;
+  uint32_t n_spheres = 0;
+  uint32_t n_mats = 0;
+  uint32_t depth = 0;
+};
+
+// Host-side result of the BVH conversion, ready to upload.
+struct HostDeviceBVH {
+  std::vector<float> inner;        // 16 floats per internal node
+  std::vector<float> tris;         // 16 floats per triangle slot
+  std::vector<uint32_t> tri_ids;
+  std::vector<uint32_t> tri_mat;
+  std::vector<float> spheres;      // 8 floats per sphere
+  std::vector<float> mats;         // 8 floats per material
+  uint32_t root = kSentinel;
+  uint32_t depth = 0;
+};
+
+// ---- host BVH builder (host_bvh.cpp) ----
+// Applies ModelSpaceToWorldSpace when models != nullptr (in place on copies).
+// Returns false with msg on invalid input.
+bool world_space(const RtTriangle64* tris, uint32_t nt, const RtSphere32* sph, uint32_t ns,
+                 const RtModel64* models, uint32_t nm, std::vector<RtTriangle64>& out_t,
+                 std::vector<RtSphere32>& out_s, std::string& msg);
+// The six S1 passes; nodes gets 2N-1 records.
+void build_bvh(const RtTriangle64* tris, uint32_t nt, const RtSphere32* sph, uint32_t ns,
+               uint32_t mode, std::vector<RtBVHNode40>& nodes);
+// Validates a reference-layout tree and converts it to the device form.
+bool convert_bvh(const RtBVHNode40* nodes, uint32_t nn, const RtTriangle64* tris, uint32_t nt,
+                 const RtSphere32* sph, uint32_t ns, const RtMaterial32* mats, uint32_t nm,
+                 uint32_t leaf_size, HostDeviceBVH& out, std::string& msg);
+// Camera of raytraceBVH.comp:50-81: out = camPos, pixel00, pixelDeltaU, pixelDeltaV.
+void camera_setup(const RtRaytraceUBO& ubo, uint32_t width, uint32_t height, float out[12]);
+
+unsigned host_threads();
+
+// Runs f(begin, end, chunk) over [0, n) split into at most host_threads()
+// contiguous chunks.
+template <class F>
+void parallel_for(size_t n, F&& f, size_t grain = 8192) {
+  unsigned T = host_threads();
+  if (T <= 1 || n < 2 * grain) {
+    f((size_t)0, n, 0u);
+    return;
+  }
+  size_t chunks = std::min<size_t>(T, (n + grain - 1) / grain);
+  size_t per = (n + chunks - 1) / chunks;
+  std::vector<std::thread> th;
+  th.reserve(chunks);
+  for (size_t c = 0; c < chunks; ++c) {
+    size_t b = c * per, e = std::min(n, b + per);
+    if (b >= e) break;
+    th.emplace_back([&f, b, e, c] { f(b, e, (unsigned)c); });
+  }
+  for (auto& t : th) t.join();
+}
+
+// ---- device side (trace.cu / render.cu) ----
+struct LaunchCfg {
+  int blocks = 0;
+  int threads = 0;
+};
+// Kernels launch on the given stream; counter is a device uint32 zeroed by the caller.
+cudaError_t launch_trace(const DeviceScene& s, const RtRay* rays, uint32_t n, RtHit* hits, uint32_t flags,
+                         uint32_t* counter, void* stream);
+cudaError_t launch_render(const DeviceScene& s, const float cam[12], uint32_t depth, uint32_t random_state,
+                          float* accum, uint32_t w, uint32_t h, uint32_t spp, uint32_t shade_mode,
+                          const float bg[3], uint32_t* counter, void* stream);
+cudaError_t launch_accum_clear(float* accum, uint32_t w, uint32_t h, void* stream);
+cudaError_t launch_resolve(const float* accum, uint32_t w, uint32_t h, uint32_t spp, float* out, void* stream);
+int device_sm_count();
+
+}  // namespace rtgb

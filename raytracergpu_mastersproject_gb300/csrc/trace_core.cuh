@@ -1,0 +1,227 @@
+// trace_core.cuh -- device traversal and intersection shared by the ray-query
+// and path-tracing kernels.
+//
+// Arithmetic contract: the translation units that include this header are
+// compiled with -fmad=false and IEEE division/square root, so each binary32
+// operation below rounds on its own in the order written -- the same contract
+// the reference's shader expressions are restated under on the host.  FMAs
+// appear only where written explicitly (fmaf), and only in box tests, whose
+// results are widened to stay conservative.
+#pragma once
+
+#include <cstdint>
+
+#include "rt_internal.h"
+
+namespace rtgb {
+namespace dev {
+
+constexpr uint32_t kNoBest = 0u;  // "no hit yet" (every leaf ref has bit31 set)
+
+// ---------------------------------------------------------------- loads ---
+__device__ __forceinline__ float4 ldg4(const void* base, uint32_t idx) {
+  return __ldg(reinterpret_cast<const float4*>(base) + idx);
+}
+__device__ __forceinline__ uint32_t fbits(float f) { return __float_as_uint(f); }
+
+// ------------------------------------------------------- triangle test ----
+// triangleHit (raytraceBVH.comp:118-149) on a precomputed 64-byte record;
+// returns true and t for a hit in [tmin, tmax].  A NaN t never hits.
+__device__ __forceinline__ bool tri_test(const void* tris, uint32_t slot, float ox, float oy, float oz,
+                                         float dx, float dy, float dz, float tmin, float tmax, float& t_out) {
+  const float4 r0 = ldg4(tris, 4u * slot + 0u);  // n.xyz, D
+  const float denom = r0.x * dx + r0.y * dy + r0.z * dz;
+  if (fabsf(denom) < 0.0001f) return false;
+  const float t = (r0.w - (r0.x * ox + r0.y * oy + r0.z * oz)) / denom;
+  if (!(t >= tmin && t <= tmax)) return false;
+  const float4 r1 = ldg4(tris, 4u * slot + 1u);  // w.xyz, v0.x
+  const float4 r2 = ldg4(tris, 4u * slot + 2u);  // v0.y, v0.z, u.x, u.y
+  const float4 r3 = ldg4(tris, 4u * slot + 3u);  // u.z, v.x, v.y, v.z
+  const float px = ox + t * dx, py = oy + t * dy, pz = oz + t * dz;
+  const float qx = px - r1.w, qy = py - r2.x, qz = pz - r2.y;
+  const float ux = r2.z, uy = r2.w, uz = r3.x;
+  const float vx = r3.y, vy = r3.z, vz = r3.w;
+  // a = dot(w, cross(q, v)); b = dot(w, cross(u, q))
+  const float cqx = qy * vz - qz * vy, cqy = qz * vx - qx * vz, cqz = qx * vy - qy * vx;
+  const float a = r1.x * cqx + r1.y * cqy + r1.z * cqz;
+  const float cux = uy * qz - uz * qy, cuy = uz * qx - ux * qz, cuz = ux * qy - uy * qx;
+  const float b = r1.x * cux + r1.y * cuy + r1.z * cuz;
+  if (a < 0.0f || b < 0.0f || a + b > 1.0f) return false;
+  t_out = t;
+  return true;
+}
+
+// sphereHit (raytraceBVH.comp:152-181) -- root only; the hit record is rebuilt
+// by the caller when it needs the normal.
+__device__ __forceinline__ bool sphere_test(const void* spheres, uint32_t idx, float ox, float oy, float oz,
+                                            float dx, float dy, float dz, float tmin, float tmax, float& t_out) {
+  const float4 s = ldg4(spheres, 2u * idx);
+  const float ocx = ox - s.x, ocy = oy - s.y, ocz = oz - s.z;
+  const float a = dx * dx + dy * dy + dz * dz;
+  const float halfB = ocx * dx + ocy * dy + ocz * dz;
+  const float c = (ocx * ocx + ocy * ocy + ocz * ocz) - (s.w * s.w);
+  const float under = (halfB * halfB) - (a * c);
+  if (under < 0.0f) return false;
+  const float rad = sqrtf(under);
+  float root = (-halfB - rad) / a;
+  if (root < tmin || root > tmax) {
+    root = (-halfB + rad) / a;
+    if (root < tmin || root > tmax) return false;
+  }
+  t_out = root;
+  return true;
+}
+
+// ---------------------------------------------------------- traversal ----
+// One ray's traversal state; kept in registers across warp refills.
+struct Trav {
+  float ox, oy, oz, dx, dy, dz;  // the ray exactly as given (triangle tests)
+  float ix, iy, iz;              // 1/d, with zero components replaced
+  float tmin, tclose;            // interval; tclose = closest hit so far
+  float cull_lo, cull_hi;        // widened interval for box culling
+  uint32_t best;                 // leaf-style ref of the closest hit (kNoBest: none)
+  uint32_t node;                 // next node to visit, or a leaf, or kSentinel
+  uint32_t leaf;                 // postponed leaf (0: none)
+  int sp;                        // stack top index; stack[0] = kSentinel
+};
+
+// Box culling margin: wider than the binary32 rounding of box and triangle
+// t values, so that a box is skipped only when it cannot hold a closer hit
+// except within the margin (a near-tie).
+constexpr float kCullRel = 1.52587890625e-05f;  // 2^-16
+constexpr float kSlabWiden = 4.76837158203125e-07f;  // 2^-21: > 3 ulps of (b-o)*(1/d)
+
+__device__ __forceinline__ void trav_set_close(Trav& s, float t) {
+  s.tclose = t;
+  s.cull_hi = fmaf(fabsf(t), kCullRel, t);
+}
+
+__device__ __forceinline__ void trav_init(Trav& s, const float4 o_tmin, const float4 d_tmax, uint32_t root,
+                                          uint32_t* stack) {
+  s.ox = o_tmin.x; s.oy = o_tmin.y; s.oz = o_tmin.z; s.tmin = o_tmin.w;
+  s.dx = d_tmax.x; s.dy = d_tmax.y; s.dz = d_tmax.z;
+  const float eps = 1e-30f;
+  s.ix = 1.0f / (fabsf(s.dx) > eps ? s.dx : copysignf(eps, s.dx));
+  s.iy = 1.0f / (fabsf(s.dy) > eps ? s.dy : copysignf(eps, s.dy));
+  s.iz = 1.0f / (fabsf(s.dz) > eps ? s.dz : copysignf(eps, s.dz));
+  s.cull_lo = fmaf(-fabsf(s.tmin), kCullRel, s.tmin);
+  trav_set_close(s, d_tmax.w);
+  s.best = kNoBest;
+  s.node = root;
+  s.leaf = 0u;
+  if (root > kSentinel) {  // the whole tree is one leaf
+    s.leaf = root;
+    s.node = kSentinel;
+  }
+  s.sp = 0;
+  stack[0] = kSentinel;
+}
+
+// Near/far parameters of one child box, robust form (b - o) * (1/d), widened.
+__device__ __forceinline__ void slab(const Trav& s, float lox, float hix, float loy, float hiy, float loz,
+                                     float hiz, float& tn, float& tf) {
+  const float x0 = (lox - s.ox) * s.ix, x1 = (hix - s.ox) * s.ix;
+  const float y0 = (loy - s.oy) * s.iy, y1 = (hiy - s.oy) * s.iy;
+  const float z0 = (loz - s.oz) * s.iz, z1 = (hiz - s.oz) * s.iz;
+  const float n = fmaxf(fmaxf(fminf(x0, x1), fminf(y0, y1)), fminf(z0, z1));
+  const float f = fminf(fminf(fmaxf(x0, x1), fmaxf(y0, y1)), fmaxf(z0, z1));
+  tn = fmaf(-fabsf(n), kSlabWiden, n);
+  tf = fmaf(fabsf(f), kSlabWiden, f);
+}
+
+__device__ __forceinline__ bool is_inner(uint32_t r) { return r < kSentinel; }
+__device__ __forceinline__ bool is_leaf(uint32_t r) { return r > kSentinel; }
+
+// Tests the primitives of one leaf ref; returns true when the ray is done
+// (any-hit found).
+template <bool ANY>
+__device__ __forceinline__ bool leaf_visit(const DeviceScene& S, Trav& s, uint32_t leaf) {
+  if (leaf & kSphereBit) {
+    const uint32_t idx = leaf & kSphereMask;
+    float t;
+    if (idx < S.n_spheres && sphere_test(S.spheres, idx, s.ox, s.oy, s.oz, s.dx, s.dy, s.dz, s.tmin, s.tclose, t)) {
+      trav_set_close(s, t);
+      s.best = leaf;
+      if (ANY) return true;
+    }
+    return false;
+  }
+  const uint32_t first = leaf & kSlotMask;
+  const uint32_t count = ((leaf >> kCountShift) & 7u) + 1u;
+  for (uint32_t k = 0; k < count; ++k) {
+    float t;
+    if (tri_test(S.tris, first + k, s.ox, s.oy, s.oz, s.dx, s.dy, s.dz, s.tmin, s.tclose, t)) {
+      trav_set_close(s, t);
+      s.best = kLeafBit | (first + k);
+      if (ANY) return true;
+    }
+  }
+  return false;
+}
+
+// Advances the traversal.  Returns true when the ray is finished.  Returns
+// false early when fewer than `refill` lanes of the warp are still traversing,
+// so that the warp can hand new rays to its idle lanes (state is kept).
+// Returns false with s.sp == -1 on stack overflow (the ray is abandoned).
+template <bool ANY, int STACK>
+__device__ __forceinline__ bool trav_run(const DeviceScene& S, Trav& s, uint32_t* stack, int refill) {
+  for (;;) {
+    // Inner nodes: descend, postponing the first leaf found.
+    while (is_inner(s.node)) {
+      const float4 a = ldg4(S.inner, 4u * s.node + 0u);
+      const float4 b = ldg4(S.inner, 4u * s.node + 1u);
+      const float4 c = ldg4(S.inner, 4u * s.node + 2u);
+      const float4 d = ldg4(S.inner, 4u * s.node + 3u);
+      float n0, f0, n1, f1;
+      slab(s, a.x, a.y, a.z, a.w, c.x, c.y, n0, f0);
+      slab(s, b.x, b.y, b.z, b.w, c.z, c.w, n1, f1);
+      const bool h0 = fmaxf(n0, s.cull_lo) <= fminf(f0, s.cull_hi);
+      const bool h1 = fmaxf(n1, s.cull_lo) <= fminf(f1, s.cull_hi);
+      const uint32_t r0 = fbits(d.x), r1 = fbits(d.y);
+      if (!h0 && !h1) {
+        s.node = stack[s.sp];
+        s.sp = s.sp > 0 ? s.sp - 1 : 0;
+      } else {
+        uint32_t first = h0 ? r0 : r1;
+        if (h0 && h1) {
+          uint32_t second = r1;
+          if (n1 < n0) {
+            first = r1;
+            second = r0;
+          }
+          if (s.sp + 1 >= STACK) {
+            s.sp = -1;
+            return false;
+          }
+          stack[++s.sp] = second;
+        }
+        s.node = first;
+      }
+      if (is_leaf(s.node) && s.leaf == 0u) {
+        s.leaf = s.node;
+        s.node = stack[s.sp];
+        s.sp = s.sp > 0 ? s.sp - 1 : 0;
+      }
+      if (__all_sync(__activemask(), s.leaf != 0u)) break;
+    }
+    // Leaves: test the postponed leaf, then any leaves popped in sequence.
+    while (s.leaf != 0u) {
+      if (leaf_visit<ANY>(S, s, s.leaf)) {
+        s.leaf = 0u;
+        s.node = kSentinel;
+        return true;
+      }
+      s.leaf = 0u;
+      if (is_leaf(s.node)) {
+        s.leaf = s.node;
+        s.node = stack[s.sp];
+        s.sp = s.sp > 0 ? s.sp - 1 : 0;
+      }
+    }
+    if (s.node == kSentinel) return true;
+    if (refill > 0 && __popc(__activemask()) < refill) return false;
+  }
+}
+
+}  // namespace dev
+}  // namespace rtgb

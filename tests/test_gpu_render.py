@@ -1,0 +1,125 @@
+"""GPU parity of the path-tracing pass (rt_render) against the CPU oracle.
+
+rt_render runs spp samples of raytraceBVH.comp:main per pixel with the
+reference RNG (random.glsl) and its alpha-channel carry; images must agree
+with the oracle within per-pixel RMSE 1e-3 at identical RNG streams.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def lit_scene(rt):
+    sph = rt.gen_icosphere(3, (0.0, 0.0, 0.0), 1.0, 0)
+    ground = rt.gen_config1()[0][-2:]
+    tris = np.concatenate([sph, ground])
+    mats = np.zeros(2, rt.MATERIAL_DTYPE)
+    mats[0]["albedo"][:3] = (0.73, 0.33, 0.25)
+    mats[0]["materialType"] = rt.MAT_DIFFUSE
+    mats[1]["albedo"][:3] = (3.0, 3.0, 3.0)
+    mats[1]["materialType"] = rt.MAT_LIGHT
+    return tris, mats
+
+
+def gpu_render(rt, torch, scene, ubo, w, h, spp, calls=1, **kw):
+    acc = torch.empty(w * h * 4, dtype=torch.float32, device="cuda")
+    rt.accum_clear(acc, w, h)
+    for _ in range(calls):
+        scene.render(ubo, acc, w, h, spp, **kw)
+    torch.cuda.synchronize()
+    return acc.cpu().numpy()
+
+
+def oracle_render(orc, tris, nodes, mats, ubo, w, h, spp, spheres=None, **kw):
+    acc = np.tile(np.array([0, 0, 0, 1], np.float32), w * h)
+    status = orc.render(orc.Scene(tris, nodes, spheres=spheres, mats=mats), ubo, acc, w, h, spp, **kw)
+    assert status == 0
+    return acc
+
+
+def rmse(a, b):
+    return float(np.sqrt(np.mean((a.astype(np.float64) - b.astype(np.float64)) ** 2)))
+
+
+@pytest.mark.parametrize("mode", [0, 1], ids=["sorted", "reference"])
+def test_reference_shading(rt, orc, cuda, mode):
+    tris, mats = lit_scene(rt)
+    ubo = rt.make_ubo((0.0, 0.5, 4.0), (0.0, 0.0, 0.0), fov=60.0, depth=5, random_state=12345)
+    w, h, spp = 96, 54, 4
+    with rt.Scene(tris, materials=mats, bvh_mode=mode) as sc:
+        img = gpu_render(rt, cuda, sc, ubo, w, h, spp)
+        ref = oracle_render(orc, tris, sc.nodes(), mats, ubo, w, h, spp)
+    assert rmse(img, ref) <= 1e-3
+    assert np.mean(img == ref) > 0.99  # bit-identical except pixels whose paths met a near-tie
+    assert img[0::4].max() > 0.1       # the light reaches the camera
+
+
+def test_samples_split_across_calls(rt, cuda):
+    """Alpha carries the RNG between samples (raytraceBVH.comp:350-372), so
+    two calls of 2 samples equal one call of 4."""
+    tris, mats = lit_scene(rt)
+    ubo = rt.make_ubo((0.0, 0.5, 4.0), (0.0, 0.0, 0.0), fov=60.0, depth=4, random_state=99)
+    with rt.Scene(tris, materials=mats) as sc:
+        a = gpu_render(rt, cuda, sc, ubo, 64, 36, 4)
+        b = gpu_render(rt, cuda, sc, ubo, 64, 36, 2, calls=2)
+    assert np.array_equal(a, b)
+
+
+def test_extended_materials_and_spheres(rt, orc, cuda):
+    tris, mats = rt.gen_spheres_scene(21, 6, 2, 0.05)
+    ground = rt.gen_config1()[0][-2:].copy()
+    ground["v0"][:, 1] = ground["v1"][:, 1] = ground["v2"][:, 1] = -9.0
+    ground["materialIndex"] = len(mats)
+    lam = np.zeros(1, rt.MATERIAL_DTYPE)
+    lam["albedo"][0][:3] = (0.5, 0.5, 0.5)
+    lam["materialType"] = rt.MAT_DIFFUSE
+    sph = np.zeros(2, rt.SPHERE_DTYPE)
+    sph["center"][:, :3] = [(0.0, 0.0, 0.0), (3.0, 1.0, 2.0)]
+    sph["radius"] = [1.5, 1.0]
+    sph["materialIndex"] = [len(mats) + 1, 2]
+    glass = np.zeros(1, rt.MATERIAL_DTYPE)
+    glass["albedo"][0][:3] = 1.0
+    glass["materialType"] = rt.MAT_DIELECTRIC
+    glass["ior"] = 1.5
+    allm = np.concatenate([mats, lam, glass])
+    allt = np.concatenate([tris, ground])
+    ubo = rt.make_ubo((0.0, 3.0, 28.0), (0.0, 0.0, 0.0), fov=40.0, depth=8, random_state=7)
+    w, h, spp = 80, 45, 3
+    bg = (0.6, 0.7, 1.0)
+    with rt.Scene(allt, spheres=sph, materials=allm) as sc:
+        img = gpu_render(rt, cuda, sc, ubo, w, h, spp, shade_mode=rt.SHADE_EXTENDED, background=bg)
+        ref = oracle_render(orc, allt, sc.nodes(), allm, ubo, w, h, spp, spheres=sph, extended=True, background=bg)
+        img_ref_mode = gpu_render(rt, cuda, sc, ubo, w, h, spp)
+        ref_ref_mode = oracle_render(orc, allt, sc.nodes(), allm, ubo, w, h, spp, spheres=sph)
+    assert rmse(img, ref) <= 1e-3
+    assert np.mean(img == ref) > 0.99
+    assert rmse(img_ref_mode, ref_ref_mode) <= 1e-3
+    assert img[0::4].max() > 0.1
+
+
+def test_resolve_and_clear(rt, orc, cuda):
+    tris, mats = lit_scene(rt)
+    ubo = rt.make_ubo((0.0, 0.5, 4.0), (0.0, 0.0, 0.0), depth=3, random_state=3)
+    w, h, spp = 48, 27, 2
+    with rt.Scene(tris, materials=mats) as sc:
+        acc = cuda.empty(w * h * 4, dtype=cuda.float32, device="cuda")
+        rt.accum_clear(acc, w, h)
+        cleared = acc.cpu().numpy().reshape(-1, 4)
+        assert np.all(cleared == np.array([0, 0, 0, 1], np.float32))
+        sc.render(ubo, acc, w, h, spp)
+        out = cuda.empty_like(acc)
+        rt.resolve(acc, w, h, spp, out)
+        cuda.cuda.synchronize()
+        ref = orc.resolve(acc.cpu().numpy(), w, h, spp)
+    assert np.array_equal(out.cpu().numpy(), ref)
+
+
+def test_render_rejects_bad_material(rt, cuda):
+    tris, mats = lit_scene(rt)
+    ubo = rt.make_ubo((0.0, 0.5, 4.0), (0.0, 0.0, 0.0))
+    with rt.Scene(tris, materials=mats[:1]) as sc:
+        acc = cuda.empty(16 * 9 * 4, dtype=cuda.float32, device="cuda")
+        with pytest.raises(rt.RtError) as e:
+            sc.render(ubo, acc, 16, 9, 1)
+        assert e.value.status == 1

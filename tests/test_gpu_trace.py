@@ -1,0 +1,216 @@
+"""GPU parity of the ray-query path (rt_trace / rt_trace_host) against the CPU oracle.
+
+The oracle restates hitBVH (raytraceBVH.comp:195-265) and triangleHit
+(:118-149).  Hit ids must match on every ray except near-ties, which the
+binary64 arbiter (oracle.arbitrate) accepts; matching hits must carry the
+bit-identical binary32 t.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def dev_trace(rt, torch, scene, rays, any_hit=False):
+    rays = np.ascontiguousarray(rays, dtype=rt.RAY_DTYPE)
+    d_rays = torch.from_numpy(rays.view(np.uint8)).cuda()
+    d_hits = torch.full((max(len(rays), 1) * 8,), 0xAB, dtype=torch.uint8, device="cuda")
+    scene.trace(d_rays, d_hits, n=len(rays), any_hit=any_hit)
+    torch.cuda.synchronize()
+    return d_hits.cpu().numpy().view(rt.HIT_DTYPE)[: len(rays)]
+
+
+def assert_parity(orc, tris, rays, ref, got):
+    arb = orc.arbitrate(tris, rays, ref, got)
+    assert not arb["unexplained"], f"unexplained mismatches at rays {arb['unexplained'][:10]} ({arb})"
+    same = ref["prim"] == got["prim"]
+    hit = same & (ref["prim"] != orc.NO_HIT)
+    assert np.array_equal(ref["t"][hit].view(np.uint32), got["t"][hit].view(np.uint32)), "t differs on matching hits"
+    miss = got["prim"] == orc.NO_HIT
+    assert np.all(np.isinf(got["t"][miss]))
+    return arb
+
+
+@pytest.mark.parametrize("mode", [0, 1], ids=["sorted", "reference"])
+def test_config1_matches_reference_order(rt, orc, cuda, mode):
+    tris, ubo, rays = rt.gen_config1()
+    with rt.Scene(tris, bvh_mode=mode) as sc:
+        got = dev_trace(rt, cuda, sc, rays)
+        ref, st = orc.trace(orc.Scene(tris, sc.nodes()), rays)
+    assert st[4] == 0
+    arb = assert_parity(orc, tris, rays, ref, got)
+    assert (got["prim"] != orc.NO_HIT).sum() > 100000
+    assert arb["mismatch"] <= 20
+
+
+@pytest.mark.parametrize("leaf", [2, 4, 8])
+def test_collapsed_leaves_same_hits(rt, orc, cuda, leaf):
+    tris, ubo, rays = rt.gen_config1()
+    with rt.Scene(tris) as base, rt.Scene(tris, leaf_size=leaf) as sc:
+        a = dev_trace(rt, cuda, base, rays)
+        b = dev_trace(rt, cuda, sc, rays)
+        assert sc.info().device_nodes < base.info().device_nodes
+        ref, _ = orc.trace(orc.Scene(tris, sc.nodes()), rays)
+    assert_parity(orc, tris, rays, ref, b)
+    assert_parity(orc, tris, rays, a, b)
+
+
+def test_soup_matches_oracle(rt, orc, cuda):
+    tris = rt.gen_soup(11, 0, 200_000, 1.0, 0.004)
+    rays = rt.gen_rays(11, 0, 300_000, 1.0, 1e-4, float("inf"))
+    with rt.Scene(tris) as sc:
+        got = dev_trace(rt, cuda, sc, rays)
+        S = orc.Scene(tris, sc.nodes())
+    can, _ = orc.trace(S, rays, canonical=True)
+    assert_parity(orc, tris, rays, can, got)
+    ref, _ = orc.trace(S, rays[:20000])
+    assert_parity(orc, tris, rays[:20000], ref, got[:20000])
+
+
+def test_any_hit_semantics(rt, orc, cuda):
+    tris = rt.gen_soup(12, 0, 100_000, 1.0, 0.004)
+    rays = rt.gen_rays(12, 0, 100_000, 1.0, 1e-4, 0.05)
+    with rt.Scene(tris) as sc:
+        anyh = dev_trace(rt, cuda, sc, rays, any_hit=True)
+        close = dev_trace(rt, cuda, sc, rays)
+        ref, _ = orc.trace(orc.Scene(tris, sc.nodes()), rays, canonical=True)
+    assert np.array_equal(anyh["prim"] != orc.NO_HIT, ref["prim"] != orc.NO_HIT)
+    assert np.array_equal(close["prim"] != orc.NO_HIT, ref["prim"] != orc.NO_HIT)
+    idx = np.nonzero(anyh["prim"] != orc.NO_HIT)[0]
+    for i in idx[:: max(1, len(idx) // 500)]:
+        t = orc.triangle_test(tris[anyh["prim"][i]], rays[i:i + 1])
+        assert t is not None and np.float32(t) == anyh["t"][i]
+        assert anyh["t"][i] >= close["t"][i]
+
+
+def test_config3_full_size(rt, orc, cuda):
+    """4,194,304 triangles, 16,777,216 rays: every ray against the oracle's
+    canonical traversal; any-hit agrees with closest-hit on which rays hit;
+    a second run is bit-identical."""
+    tris = rt.gen_soup(3, 0, 4_194_304, 1.0, 0.002)
+    rays = rt.gen_rays(3, 0, 16_777_216, 1.0, 1e-4, float("inf"))
+    with rt.Scene(tris) as sc:
+        got = dev_trace(rt, cuda, sc, rays)
+        again = dev_trace(rt, cuda, sc, rays)
+        anyh = dev_trace(rt, cuda, sc, rays, any_hit=True)
+        S = orc.Scene(tris, sc.nodes())
+    assert np.array_equal(got.view(np.uint64), again.view(np.uint64))
+    assert np.array_equal(got["prim"] != orc.NO_HIT, anyh["prim"] != orc.NO_HIT)
+    can, _ = orc.trace(S, rays, canonical=True)
+    arb = assert_parity(orc, tris, rays, can, got)
+    assert arb["mismatch"] < 1000
+    ref, _ = orc.trace(S, rays[:8192])
+    assert_parity(orc, tris, rays[:8192], ref, got[:8192])
+
+
+def test_trace_host_matches_device(rt, cuda):
+    tris = rt.gen_soup(13, 0, 50_000, 1.0, 0.004)
+    rays = rt.gen_rays(13, 0, 5_000_000, 1.0, 1e-4, float("inf"))
+    with rt.Scene(tris) as sc:
+        a = dev_trace(rt, cuda, sc, rays)
+        b = sc.trace_host(rays)
+        pinned = cuda.from_numpy(rays.view(np.uint8)).pin_memory()
+        c = sc.trace_host(pinned.numpy().view(rt.RAY_DTYPE))
+    assert np.array_equal(a.view(np.uint64), b.view(np.uint64))
+    assert np.array_equal(a.view(np.uint64), c.view(np.uint64))
+
+
+def test_caller_supplied_nodes(rt, orc, cuda):
+    tris, ubo, rays = rt.gen_config1()
+    nodes, _, _, _ = orc.build_bvh(tris, mode=1)
+    with rt.Scene(tris, nodes=nodes) as sc, rt.Scene(tris, bvh_mode=1) as sc2:
+        assert np.array_equal(sc.nodes().view(np.uint8), nodes.view(np.uint8))
+        a = dev_trace(rt, cuda, sc, rays)
+        b = dev_trace(rt, cuda, sc2, rays)
+    assert np.array_equal(a.view(np.uint64), b.view(np.uint64))
+
+
+def test_spheres_and_models(rt, orc, cuda):
+    tris = rt.gen_icosphere(2, (0.0, 0.0, 0.0), 1.0, 0)
+    tris["modelIndex"] = 0
+    sph = np.zeros(3, rt.SPHERE_DTYPE)
+    sph["center"][:, :3] = [(2.5, 0, 0), (-2.5, 0.5, 0), (0, 2.5, -1)]
+    sph["radius"] = [0.7, 0.5, 0.9]
+    sph["modelIndex"] = [1, 1, 0]
+    models = np.zeros(2, rt.MODEL_DTYPE)
+    models[0]["m"] = np.eye(4, dtype=np.float32).T.ravel()
+    m = np.eye(4, dtype=np.float32)
+    m[:3, 3] = (0.25, -0.5, 0.125)
+    m[0, 0] = 1.5
+    models[1]["m"] = m.T.ravel()  # column-major
+    ubo = rt.make_ubo((0.0, 0.5, 6.0), (0.0, 0.0, 0.0), fov=70.0)
+    rays = rt.gen_camera_rays(ubo, 160, 90)
+    with rt.Scene(tris, spheres=sph, models=models) as sc:
+        got = dev_trace(rt, cuda, sc, rays)
+        nodes = sc.nodes()
+    onodes, _, _, _ = orc.build_bvh(tris, sph, mode=0, models=models["m"])
+    assert np.array_equal(nodes.view(np.uint8), onodes.view(np.uint8))
+    # the oracle traces world-space records: transform them the same way
+    wt, ws = world(rt, tris, sph, models)
+    ref, _ = orc.trace(orc.Scene(wt, nodes, spheres=ws), rays)
+    assert np.array_equal(ref["prim"], got["prim"])
+    hit = ref["prim"] != orc.NO_HIT
+    assert np.array_equal(ref["t"][hit].view(np.uint32), got["t"][hit].view(np.uint32))
+    assert ((got["prim"] & rt.HIT_SPHERE_BIT) != 0).sum() > 100
+
+
+def world(rt, tris, sph, models):
+    """ModelSpaceToWorldSpace.comp:32-48 in numpy binary32, left-to-right sums."""
+    M = models["m"].reshape(-1, 4, 4)  # [model][column][row]
+
+    def xf(m, v):
+        out = np.zeros(4, np.float32)
+        for r in range(4):
+            acc = np.float32(m[0, r] * v[0])
+            acc = np.float32(acc + np.float32(m[1, r] * v[1]))
+            acc = np.float32(acc + np.float32(m[2, r] * v[2]))
+            acc = np.float32(acc + np.float32(m[3, r] * np.float32(1.0)))
+            out[r] = acc
+        return out
+
+    wt = tris.copy()
+    for i in range(len(wt)):
+        for k in ("v0", "v1", "v2"):
+            wt[i][k] = xf(M[wt[i]["modelIndex"]], wt[i][k])
+    ws = sph.copy()
+    for i in range(len(ws)):
+        ws[i]["center"] = xf(M[ws[i]["modelIndex"]], ws[i]["center"])
+    return wt, ws
+
+
+def test_edge_cases(rt, orc, cuda):
+    # one triangle; axis-aligned and grazing rays; ray starting on the triangle; tmax < tmin
+    t = np.zeros(2, rt.TRIANGLE_DTYPE)
+    t[0]["v0"][:3] = (0, 0, 0)
+    t[0]["v1"][:3] = (1, 0, 0)
+    t[0]["v2"][:3] = (0, 1, 0)
+    t[1]["v0"][:3] = (5, 5, 5)  # zero-area: defined as never hit
+    t[1]["v1"][:3] = (5, 5, 5)
+    t[1]["v2"][:3] = (6, 6, 6)
+    r = np.zeros(8, rt.RAY_DTYPE)
+    r["tmin"] = 0.0
+    r["tmax"] = np.inf
+    r[0]["org"], r[0]["dir"] = (0.25, 0.25, 1.0), (0, 0, -1)      # straight down the z axis
+    r[1]["org"], r[1]["dir"] = (0.25, 0.25, -1.0), (0, 0, 1)      # from below
+    r[2]["org"], r[2]["dir"] = (-1, 0.5, 0.0), (1, 0, 0)          # in the plane: parallel
+    r[3]["org"], r[3]["dir"] = (0.2, 0.2, 0.0), (0, 0, 1)         # starts on the triangle
+    r[4]["org"], r[4]["dir"] = (0.25, 0.25, 1.0), (0, 0, -1)
+    r[4]["tmax"] = 0.5                                            # hit beyond tmax
+    r[5]["org"], r[5]["dir"] = (0.25, 0.25, 1.0), (0, 0, -1)
+    r[5]["tmin"], r[5]["tmax"] = 2.0, 1.0                         # empty interval
+    r[6]["org"], r[6]["dir"] = (5.5, 5.5, 4.0), (0, 0, 1)         # through the zero-area one
+    r[7]["org"], r[7]["dir"] = (1.0, 0.0, 1.0), (0, 0, -1)        # exactly on a vertex
+    with rt.Scene(t) as sc:
+        got = dev_trace(rt, cuda, sc, r)
+        ref, _ = orc.trace(orc.Scene(t, sc.nodes()), r)
+    assert np.array_equal(got["prim"], ref["prim"]), (got, ref)
+    assert list(got["prim"][:2]) == [0, 0]
+    assert got["prim"][2] == orc.NO_HIT and got["prim"][4] == orc.NO_HIT and got["prim"][5] == orc.NO_HIT
+    assert got["prim"][6] == orc.NO_HIT
+    hit = ref["prim"] != orc.NO_HIT
+    assert np.array_equal(got["t"][hit], ref["t"][hit])
+    # empty scene: every ray misses; zero rays is a no-op
+    with rt.Scene(np.zeros(0, rt.TRIANGLE_DTYPE)) as empty:
+        g = dev_trace(rt, cuda, empty, r)
+        assert np.all(g["prim"] == orc.NO_HIT)
+        empty.trace(cuda.empty(0, dtype=cuda.uint8, device="cuda"), cuda.empty(0, dtype=cuda.uint8, device="cuda"), n=0)
