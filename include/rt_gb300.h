@@ -218,6 +218,32 @@ rt_status rt_trace(rt_scene* scene, const RtRay* d_rays, uint32_t n, RtHit* d_hi
 rt_status rt_trace_host(rt_scene* scene, const RtRay* h_rays, uint32_t n, RtHit* h_hits,
                         uint32_t flags, void* stream);
 
+/* rt_trace without any device allocation.  No counterpart in the reference.
+ *
+ * Who needs it: host applications that must not call cudaMalloc while they
+ * trace -- an engine that reserves the device's memory up front and hands
+ * every byte out from its own pool, or a frame loop that cannot afford the
+ * device-wide synchronisation a cudaMalloc may cause.  rt_trace allocates a
+ * small per-stream workspace (its ray-queue counter) with cudaMalloc the
+ * first time it sees a stream; this entry point never allocates.  The scene
+ * (created beforehand; creation does allocate), the rays and the hits are
+ * the caller's, as for rt_trace, and the results are identical.
+ *
+ * Its scratch is a file-scope device array of RT_NOALLOC_SCRATCH_BYTES that
+ * every GPU which loads the library holds until the process exits.  The
+ * first call on a device, with that device current, looks up the array's
+ * device address (cudaGetSymbolAddress); make that first call before any
+ * stream capture.  All calls share the one array and it keeps the last
+ * call's contents (each call zeroes what must start at zero): calls that
+ * overlap on the GPU -- on different streams or from different host
+ * threads -- race and must be serialised by the caller.
+ * Limit: n <= RT_NOALLOC_MAX_RAYS per call (the scratch counter is 32-bit);
+ * larger n returns RT_EINVAL. */
+#define RT_NOALLOC_SCRATCH_BYTES 256u
+#define RT_NOALLOC_MAX_RAYS 0x80000000u
+rt_status rt_trace_noalloc(rt_scene* scene, const RtRay* d_rays, uint32_t n, RtHit* d_hits,
+                           uint32_t flags, void* stream);
+
 /* ----------------------------------------------------------------- render */
 enum {
   RT_SHADE_REFERENCE = 0, /* LIGHT emits, DIFFUSE scatters, others terminate, background 0 */

@@ -29,6 +29,7 @@ namespace rtgb {
 
 static thread_local std::string g_error;
 void set_error(const std::string& msg) { g_error = msg; }
+const DeviceScene* scene_device(const rt_scene* scene) { return &scene->d; }
 
 static rt_status cuda_fail(cudaError_t e, const char* what) {
   set_error(std::string(what) + ": " + cudaGetErrorString(e));

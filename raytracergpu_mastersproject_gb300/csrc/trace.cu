@@ -7,6 +7,8 @@
 // that finished whenever fewer than kRefill lanes are still busy.
 #include <cuda_runtime.h>
 
+#include <mutex>
+
 #include "trace_core.cuh"
 
 namespace rtgb {
@@ -110,4 +112,74 @@ cudaError_t launch_trace(const DeviceScene& s, const RtRay* rays, uint32_t n, Rt
              : launch_variant<false, 128>(s, rays, n, hits, counter, st);
 }
 
+// ---- allocation-free ray queries (rt_trace_noalloc) ----
+// Scratch of rt_trace_noalloc: word 0 is the persistent kernel's ray-queue
+// counter, word 1 a status word.  Every device that loads the library holds
+// this array until the process exits; all calls share it.
+static __device__ __align__(256) uint32_t g_noalloc_scratch[RT_NOALLOC_SCRATCH_BYTES / sizeof(uint32_t)];
+
+namespace {
+constexpr int kMaxDevices = 64;
+std::mutex g_noalloc_mu;
+uint32_t* g_noalloc_ptr[kMaxDevices] = {};
+}  // namespace
+
+const DeviceScene* scene_device(const rt_scene* scene);
+void set_error(const std::string& msg);
+
 }  // namespace rtgb
+
+extern "C" rt_status rt_trace_noalloc(rt_scene* scene, const RtRay* d_rays, uint32_t n, RtHit* d_hits,
+                                      uint32_t flags, void* stream) {
+  using namespace rtgb;
+  if (!scene || (n && (!d_rays || !d_hits)) || flags > RT_TRACE_ANY) {
+    set_error("rt_trace_noalloc: bad argument");
+    return RT_EINVAL;
+  }
+  if (n > RT_NOALLOC_MAX_RAYS) {
+    set_error("rt_trace_noalloc: " + std::to_string(n) + " rays exceed the maximum of " +
+              std::to_string(RT_NOALLOC_MAX_RAYS) + " per call (the scratch ray-queue counter is 32-bit)");
+    return RT_EINVAL;
+  }
+  if (n == 0) return RT_OK;
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) {
+    set_error(std::string("rt_trace_noalloc: cudaGetDevice: ") + cudaGetErrorString(e));
+    return RT_ECUDA;
+  }
+  if (dev < 0 || dev >= kMaxDevices) {
+    set_error("rt_trace_noalloc: device ordinal above 63");
+    return RT_EINVAL;
+  }
+  uint32_t* scratch = nullptr;
+  {
+    // Set-up, once per device, with that device current: the host-side name
+    // g_noalloc_scratch is not a device address, so resolve the symbol.
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
+    if (!g_noalloc_ptr[dev]) {
+      void* p = nullptr;
+      e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+      if (e != cudaSuccess || !p) {
+        set_error(std::string("rt_trace_noalloc: cudaGetSymbolAddress: ") + cudaGetErrorString(e));
+        return RT_ECUDA;
+      }
+      g_noalloc_ptr[dev] = static_cast<uint32_t*>(p);
+    }
+    scratch = g_noalloc_ptr[dev];
+  }
+  cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+  // The array keeps the previous call's contents: the queue counter and the
+  // status word must start at zero.
+  e = cudaMemsetAsync(scratch, 0, 2 * sizeof(uint32_t), st);
+  if (e != cudaSuccess) {
+    set_error(std::string("rt_trace_noalloc: memset: ") + cudaGetErrorString(e));
+    return RT_ECUDA;
+  }
+  e = launch_trace(*scene_device(scene), d_rays, n, d_hits, flags, scratch, stream);
+  if (e != cudaSuccess) {
+    set_error(std::string("rt_trace_noalloc: launch: ") + cudaGetErrorString(e));
+    return RT_ECUDA;
+  }
+  return RT_OK;
+}
