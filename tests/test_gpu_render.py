@@ -123,3 +123,16 @@ def test_render_rejects_bad_material(rt, cuda):
         with pytest.raises(rt.RtError) as e:
             sc.render(ubo, acc, 16, 9, 1)
         assert e.value.status == 1
+
+
+def test_golden_accumulator_on_gpu(rt, cuda):
+    from pathlib import Path
+
+    g = np.load(Path(__file__).resolve().parent / "golden" / "small_scene.npz")
+    tris = g["tris"].view(rt.TRIANGLE_DTYPE)
+    mats = g["mats"].view(rt.MATERIAL_DTYPE)
+    ubo = rt.RaytracingUBO.from_buffer_copy(g["ubo"].tobytes())
+    w, h, spp = (int(v) for v in g["render_wh_spp"])
+    with rt.Scene(tris, materials=mats) as sc:
+        img = gpu_render(rt, cuda, sc, ubo, w, h, spp)
+    assert rmse(img, g["accum"]) <= 1e-3

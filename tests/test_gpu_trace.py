@@ -214,3 +214,24 @@ def test_edge_cases(rt, orc, cuda):
         g = dev_trace(rt, cuda, empty, r)
         assert np.all(g["prim"] == orc.NO_HIT)
         empty.trace(cuda.empty(0, dtype=cuda.uint8, device="cuda"), cuda.empty(0, dtype=cuda.uint8, device="cuda"), n=0)
+
+
+def test_golden_fixtures_on_gpu(rt, orc, cuda):
+    from pathlib import Path
+
+    g = np.load(Path(__file__).resolve().parent / "golden" / "small_scene.npz")
+    tris = g["tris"].view(rt.TRIANGLE_DTYPE)
+    rays = g["rays"].view(rt.RAY_DTYPE)
+    for mode, key in ((0, "sorted"), (1, "reference")):
+        with rt.Scene(tris, bvh_mode=mode) as sc:
+            assert np.array_equal(sc.nodes().view(np.uint8), g[f"nodes_{key}"])
+            got = dev_trace(rt, cuda, sc, rays)
+            want = g[f"hits_{key}"].view(rt.HIT_DTYPE)
+            assert_parity(orc, tris, rays, want, got)
+            anyh = dev_trace(rt, cuda, sc, rays, any_hit=True)
+            assert np.array_equal(anyh["prim"] != rt.NO_HIT, want["prim"] != rt.NO_HIT)
+    s = np.load(Path(__file__).resolve().parent / "golden" / "soup_small.npz")
+    st, sr = s["tris"].view(rt.TRIANGLE_DTYPE), s["rays"].view(rt.RAY_DTYPE)
+    with rt.Scene(st) as sc:
+        got = dev_trace(rt, cuda, sc, sr)
+    assert_parity(orc, st, sr, s["hits"].view(rt.HIT_DTYPE), got)
