@@ -55,6 +55,7 @@ def parse():
     p.add_argument("--tris", type=int, default=N_TRIS)
     p.add_argument("--rays", type=int, default=N_RAYS)
     p.add_argument("--leaf-size", type=int, default=0)
+    p.add_argument("--node-width", type=int, default=0, help="device BVH width (2 or 4; 0 = library default)")
     p.add_argument("--cpu-sample", type=int, default=CPU_SAMPLE)
     p.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     p.add_argument("--no-e2e", action="store_true")
@@ -217,7 +218,7 @@ def run_ours(args):
         import torch.distributed as dist
         dist.init_process_group("nccl")
     tris, rays = workload(args.tris, args.rays)
-    scene = rt.Scene(tris, leaf_size=args.leaf_size)
+    scene = rt.Scene(tris, leaf_size=args.leaf_size, node_width=args.node_width)
     info = scene.info()
     n = len(rays)
     d_rays = torch.from_numpy(rays.view(np.uint8)).cuda()
@@ -231,6 +232,7 @@ def run_ours(args):
     for _ in range(args.warmup):
         scene.trace(d_rays, d_hits)
     torch.cuda.synchronize()
+    gpu_nodes, gpu_tests = scene.trace_count(d_rays, d_hits)
     clocks = ClockSampler(local)
     clocks.start()
     time.sleep(0.5)
@@ -300,7 +302,9 @@ def run_ours(args):
                 "traffic": None, "peak_kind": peak_kind,
                 "bytes_per_ray": b_ray, "node_boxes_per_ray": counts["node_boxes_per_ray"],
                 "tri_tests_per_ray": counts["tri_tests_per_ray"],
-                "kernel": "k_trace<closest> (persistent warps, BVH2 child-box nodes)",
+                "kernel": f"k_trace<closest> (persistent warps, {info.node_width}-wide nodes)",
+                "gpu_node_fetches_per_ray": gpu_nodes / n, "gpu_prim_tests_per_ray": gpu_tests / n,
+                "fetched_bytes_per_ray": 40 + 64 * gpu_nodes / n + 64 * gpu_tests / n,
                 "avg_launch_ms": avg_launch * 1e3}
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
@@ -309,7 +313,8 @@ def run_ours(args):
                        if (args.tris, args.rays) == (N_TRIS, N_RAYS) else
                        f"config-3 shape: {args.tris} triangles, {args.rays} rays, closest-hit",
                        "triangles": args.tris, "rays": n, "bvh": "host LBVH, sorted leaves",
-                       "leaf_size": info.leaf_size, "device_nodes": info.device_nodes, "bvh_depth": info.depth,
+                       "leaf_size": info.leaf_size, "node_width": info.node_width,
+                       "device_nodes": info.device_nodes, "bvh_depth": info.depth, "stack_need": info.stack_need,
                        "l2": "inputs larger than L2 (rays 512 MiB, nodes+triangles 512 MiB); no flush",
                        "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU"},
             "roofline": roof, "cpu_baseline": cpu_base, "e2e": e2e, "clocks": clk,

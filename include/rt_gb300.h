@@ -164,7 +164,8 @@ typedef struct RtSceneDesc {
   const RtBVHNode40* nodes;       /* host; NULL = build on the host (bvh_mode) */
   uint32_t num_nodes;             /* 2*(num_triangles+num_spheres)-1 when nodes != NULL */
   uint32_t bvh_mode;              /* RT_BVH_SORTED | RT_BVH_REFERENCE */
-  uint32_t leaf_size;             /* max triangles per device leaf after collapsing; 0 = default */
+  uint32_t leaf_size;             /* max triangles per device leaf after collapsing; 0 = default (1) */
+  uint32_t node_width;            /* device BVH width: 2 (binary) or 4 (quantised); 0 = default (4) */
 } RtSceneDesc;
 
 typedef struct RtSceneInfo {
@@ -173,11 +174,13 @@ typedef struct RtSceneInfo {
   uint32_t num_materials;
   uint32_t num_nodes;          /* reference-layout node count, 2N-1 */
   uint32_t device_nodes;       /* internal nodes of the device BVH */
-  uint32_t depth;              /* longest root-to-leaf path of the device BVH */
+  uint32_t depth;              /* longest root-to-leaf path of the device BVH (inner nodes) */
   uint32_t leaf_size;
   uint32_t bvh_mode;
   uint64_t device_bytes;       /* device memory held by the scene */
   double build_seconds;        /* host BVH build + conversion time */
+  uint32_t node_width;         /* 2 or 4 */
+  uint32_t stack_need;         /* worst-case traversal stack entries */
 } RtSceneInfo;
 
 /* Replaces the scene upload + S1 BVH build of the reference
@@ -217,6 +220,12 @@ rt_status rt_trace(rt_scene* scene, const RtRay* d_rays, uint32_t n, RtHit* d_hi
  * when h_hits is filled. */
 rt_status rt_trace_host(rt_scene* scene, const RtRay* h_rays, uint32_t n, RtHit* h_hits,
                         uint32_t flags, void* stream);
+
+/* rt_trace plus work counters, for measurement (no counterpart in the
+ * reference): h_counts[0] = inner BVH nodes fetched, h_counts[1] = primitives
+ * tested, summed over the n rays.  Synchronous. */
+rt_status rt_trace_count(rt_scene* scene, const RtRay* d_rays, uint32_t n, RtHit* d_hits, uint32_t flags,
+                         void* stream, uint64_t* h_counts);
 
 /* rt_trace without any device allocation.  No counterpart in the reference.
  *

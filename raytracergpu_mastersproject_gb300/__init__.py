@@ -71,14 +71,15 @@ class _SceneDesc(C.Structure):
     _fields_ = [("triangles", C.c_void_p), ("num_triangles", C.c_uint32), ("spheres", C.c_void_p),
                 ("num_spheres", C.c_uint32), ("materials", C.c_void_p), ("num_materials", C.c_uint32),
                 ("models", C.c_void_p), ("num_models", C.c_uint32), ("nodes", C.c_void_p),
-                ("num_nodes", C.c_uint32), ("bvh_mode", C.c_uint32), ("leaf_size", C.c_uint32)]
+                ("num_nodes", C.c_uint32), ("bvh_mode", C.c_uint32), ("leaf_size", C.c_uint32),
+                ("node_width", C.c_uint32)]
 
 
 class SceneInfo(C.Structure):
     _fields_ = [("num_triangles", C.c_uint32), ("num_spheres", C.c_uint32), ("num_materials", C.c_uint32),
                 ("num_nodes", C.c_uint32), ("device_nodes", C.c_uint32), ("depth", C.c_uint32),
                 ("leaf_size", C.c_uint32), ("bvh_mode", C.c_uint32), ("device_bytes", C.c_uint64),
-                ("build_seconds", C.c_double)]
+                ("build_seconds", C.c_double), ("node_width", C.c_uint32), ("stack_need", C.c_uint32)]
 
 
 class _RenderOptions(C.Structure):
@@ -101,6 +102,7 @@ SIGNATURES = {
     "rt_build_bvh": (_I, [_P, _U32, _P, _U32, _P, _U32, _U32, _P]),
     "rt_trace": (_I, [_P, _P, _U32, _P, _U32, _P]),
     "rt_trace_host": (_I, [_P, _P, _U32, _P, _U32, _P]),
+    "rt_trace_count": (_I, [_P, _P, _U32, _P, _U32, _P, C.POINTER(_U64)]),
     "rt_render": (_I, [_P, C.POINTER(RaytracingUBO), _P, _U32, _U32, _U32, C.POINTER(_RenderOptions), _P]),
     "rt_accum_clear": (_I, [_P, _U32, _U32, _P]),
     "rt_resolve": (_I, [_P, _U32, _U32, _U32, _P, _P]),
@@ -175,10 +177,11 @@ class Scene:
     spheres, materials, models, nodes: optional arrays of the record dtypes
     bvh_mode: BVH_SORTED (default) or BVH_REFERENCE (the reference's leaf order)
     leaf_size: max triangles per device leaf (1..8); 0 = library default
+    node_width: device BVH width, 2 (binary) or 4 (quantised 4-wide); 0 = library default
     """
 
     def __init__(self, triangles, spheres=None, materials=None, models=None, nodes=None,
-                 bvh_mode: int = BVH_SORTED, leaf_size: int = 0):
+                 bvh_mode: int = BVH_SORTED, leaf_size: int = 0, node_width: int = 0):
         L = lib()
         tri = np.ascontiguousarray(triangles, dtype=TRIANGLE_DTYPE) if triangles is not None else np.zeros(0, TRIANGLE_DTYPE)
         sph = np.ascontiguousarray(spheres, dtype=SPHERE_DTYPE) if spheres is not None else np.zeros(0, SPHERE_DTYPE)
@@ -187,7 +190,7 @@ class Scene:
         nod = np.ascontiguousarray(nodes, dtype=NODE_DTYPE) if nodes is not None else None
         d = _SceneDesc(_ptr(tri), len(tri), _ptr(sph), len(sph), _ptr(mat), len(mat),
                        _ptr(mod), 0 if mod is None else len(mod), _ptr(nod), 0 if nod is None else len(nod),
-                       bvh_mode, leaf_size)
+                       bvh_mode, leaf_size, node_width)
         h = C.c_void_p()
         _check(L.rt_scene_create_ex(C.byref(d), C.byref(h)), "rt_scene_create_ex")
         self._h = h
@@ -217,6 +220,15 @@ class Scene:
             n = rays.numel() * rays.element_size() // RAY_DTYPE.itemsize
         _check(lib().rt_trace(self.handle, _ptr(rays), n, _ptr(hits), TRACE_ANY if any_hit else TRACE_CLOSEST,
                               _stream_handle(stream)), "rt_trace")
+
+    def trace_count(self, rays, hits, n: int | None = None, any_hit: bool = False, stream=None) -> tuple[int, int]:
+        """rt_trace with work counters -> (inner nodes fetched, primitives tested)."""
+        if n is None:
+            n = rays.numel() * rays.element_size() // RAY_DTYPE.itemsize
+        c = (_U64 * 2)()
+        _check(lib().rt_trace_count(self.handle, _ptr(rays), n, _ptr(hits), TRACE_ANY if any_hit else TRACE_CLOSEST,
+                                    _stream_handle(stream), c), "rt_trace_count")
+        return int(c[0]), int(c[1])
 
     def trace_host(self, rays: np.ndarray, any_hit: bool = False, out: np.ndarray | None = None, stream=None) -> np.ndarray:
         """Host rays in, host hits out; copies overlap with tracing inside the library."""

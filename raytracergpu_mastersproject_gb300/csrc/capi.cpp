@@ -157,12 +157,24 @@ rt_status rt_scene_create_ex(const RtSceneDesc* desc, rt_scene** out_scene) {
     build_bvh(wt.data(), nt, ws.data(), ns, desc->bvh_mode, sc->nodes40);
   }
   HostDeviceBVH hb;
+  uint32_t width = desc->node_width ? desc->node_width : kDefaultWidth;
+  if (width != 2 && width != 4) {
+    set_error("rt_scene_create_ex: node_width must be 0, 2 or 4");
+    return RT_EINVAL;
+  }
   if (!convert_bvh(sc->nodes40.data(), (uint32_t)sc->nodes40.size(), wt.data(), nt, ws.data(), ns, desc->materials, nm,
-                   desc->leaf_size, hb, msg)) {
+                   desc->leaf_size, width, hb, msg)) {
     set_error("rt_scene_create_ex: " + msg);
     return RT_EINVAL;
   }
-  if (hb.depth >= 127u) {
+  if (hb.width == 4 && hb.stack_need > 192u) {  // too deep for the wide stack: binary form
+    if (!convert_bvh(sc->nodes40.data(), (uint32_t)sc->nodes40.size(), wt.data(), nt, ws.data(), ns, desc->materials,
+                     nm, desc->leaf_size, 2, hb, msg)) {
+      set_error("rt_scene_create_ex: " + msg);
+      return RT_EINVAL;
+    }
+  }
+  if (hb.width == 2 && hb.stack_need > 128u) {
     set_error("rt_scene_create_ex: BVH depth " + std::to_string(hb.depth) + " exceeds the 127-level stack");
     return RT_ESTACK;
   }
@@ -209,6 +221,8 @@ rt_status rt_scene_create_ex(const RtSceneDesc* desc, rt_scene** out_scene) {
   sc->d.n_spheres = ns;
   sc->d.n_mats = nm;
   sc->d.depth = hb.depth;
+  sc->d.width = hb.width;
+  sc->d.stack_need = hb.stack_need;
   RtSceneInfo& inf = sc->info;
   inf.num_triangles = nt;
   inf.num_spheres = ns;
@@ -220,6 +234,8 @@ rt_status rt_scene_create_ex(const RtSceneDesc* desc, rt_scene** out_scene) {
   inf.bvh_mode = desc->bvh_mode;
   inf.device_bytes = total;
   inf.build_seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  inf.node_width = hb.width;
+  inf.stack_need = hb.stack_need;
   *out_scene = sc.release();
   return RT_OK;
 }
@@ -286,6 +302,32 @@ rt_status rt_trace(rt_scene* scene, const RtRay* d_rays, uint32_t n, RtHit* d_hi
   if (e != cudaSuccess) return cuda_fail(e, "rt_trace: memset");
   e = launch_trace(scene->d, d_rays, n, d_hits, flags, w->counters, stream);
   if (e != cudaSuccess) return cuda_fail(e, "rt_trace: launch");
+  return RT_OK;
+}
+
+rt_status rt_trace_count(rt_scene* scene, const RtRay* d_rays, uint32_t n, RtHit* d_hits, uint32_t flags,
+                         void* stream, uint64_t* h_counts) {
+  if (!scene || !h_counts || (n && (!d_rays || !d_hits)) || flags > RT_TRACE_ANY || n > 0x80000000u) {
+    set_error("rt_trace_count: bad argument");
+    return RT_EINVAL;
+  }
+  h_counts[0] = h_counts[1] = 0;
+  if (n == 0) return RT_OK;
+  cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+  Workspace* w = nullptr;
+  rt_status s = workspace(st, &w);
+  if (s != RT_OK) return s;
+  cudaError_t e = cudaMemsetAsync(w->counters, 0, 64 * sizeof(uint32_t), st);
+  if (e != cudaSuccess) return cuda_fail(e, "rt_trace_count: memset");
+  unsigned long long* stats = reinterpret_cast<unsigned long long*>(w->counters + 8);
+  e = launch_trace_tuned(scene->d, d_rays, n, d_hits, flags, w->counters, stream, default_tuning(), stats);
+  if (e != cudaSuccess) return cuda_fail(e, "rt_trace_count: launch");
+  unsigned long long hc[2] = {0, 0};
+  e = cudaMemcpyAsync(hc, stats, sizeof(hc), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return cuda_fail(e, "rt_trace_count: read counters");
+  h_counts[0] = hc[0];
+  h_counts[1] = hc[1];
   return RT_OK;
 }
 

@@ -348,8 +348,13 @@ static inline float bits_f(uint32_t u) {
 
 bool convert_bvh(const RtBVHNode40* nodes, uint32_t nn, const RtTriangle64* tris, uint32_t nt,
                  const RtSphere32* sph, uint32_t ns, const RtMaterial32* mats, uint32_t nm,
-                 uint32_t leaf_size, HostDeviceBVH& out, std::string& msg) {
+                 uint32_t leaf_size, uint32_t width, HostDeviceBVH& out, std::string& msg) {
   out = HostDeviceBVH();
+  if (width == 0) width = kDefaultWidth;
+  if (width != 2 && width != 4) {
+    msg = "node width must be 2 or 4";
+    return false;
+  }
   if (leaf_size == 0) leaf_size = kDefaultLeafSize;
   if (leaf_size > kMaxLeafSize) {
     msg = "leaf_size above " + std::to_string(kMaxLeafSize);
@@ -451,20 +456,23 @@ bool convert_bvh(const RtBVHNode40* nodes, uint32_t nn, const RtTriangle64* tris
     return EMPTY;
   };
 
-  // Pass C: device indices, preorder over the kept internal nodes.
-  std::vector<uint32_t> dev(nn, NONE);
-  std::vector<uint32_t> kept;
-  std::vector<std::pair<uint32_t, uint32_t>> st2;  // (node, depth)
-  uint32_t maxdepth = 0;
-  auto ref_of = [&](uint32_t x) -> uint32_t {
+  auto ref_of = [&](uint32_t x, const std::vector<uint32_t>& dev) -> uint32_t {
     if (is_leaf(x)) return leaf_ref(x);
     if (collapsible(x)) return kLeafBit | ((cnt[x] - 1u) << kCountShift) | first[x];
     return dev[x];
   };
-  if (is_leaf(0) || collapsible(0)) {
-    out.root = ref_of(0);
+  auto expandable = [&](uint32_t x) { return !is_leaf(x) && !collapsible(x); };
+  std::vector<uint32_t> dev(nn, NONE);
+  out.width = width;
+  if (!expandable(0)) {
+    out.root = ref_of(0, dev);
     out.depth = 0;
-  } else {
+    out.stack_need = 1;
+  } else if (width == 2) {
+    // Binary device tree: the kept internal nodes in left-first preorder.
+    std::vector<uint32_t> kept;
+    std::vector<std::pair<uint32_t, uint32_t>> st2;  // (node, depth)
+    uint32_t maxdepth = 0;
     st2.push_back({0u, 1u});
     while (!st2.empty()) {
       auto [x, d] = st2.back();
@@ -473,30 +481,140 @@ bool convert_bvh(const RtBVHNode40* nodes, uint32_t nn, const RtTriangle64* tris
       kept.push_back(x);
       maxdepth = std::max(maxdepth, d);
       const RtBVHNode40& nd = nodes[x];
-      if (!is_leaf(nd.right) && !collapsible(nd.right)) st2.push_back({nd.right, d + 1});
-      if (!is_leaf(nd.left) && !collapsible(nd.left)) st2.push_back({nd.left, d + 1});
+      if (expandable(nd.right)) st2.push_back({nd.right, d + 1});
+      if (expandable(nd.left)) st2.push_back({nd.left, d + 1});
     }
     out.root = 0;
     out.depth = maxdepth;
-  }
-
-  // Pass D: device nodes.
-  out.inner.resize(16 * kept.size());
-  parallel_for(kept.size(), [&](size_t b, size_t e, unsigned) {
-    for (size_t i = b; i < e; ++i) {
-      const RtBVHNode40& nd = nodes[kept[i]];
-      const RtBVHNode40& L = nodes[nd.left];
-      const RtBVHNode40& R = nodes[nd.right];
-      float* o = &out.inner[16 * i];
-      o[0] = L.minX; o[1] = L.maxX; o[2] = L.minY; o[3] = L.maxY;
-      o[4] = R.minX; o[5] = R.maxX; o[6] = R.minY; o[7] = R.maxY;
-      o[8] = L.minZ; o[9] = L.maxZ; o[10] = R.minZ; o[11] = R.maxZ;
-      o[12] = bits_f(ref_of(nd.left));
-      o[13] = bits_f(ref_of(nd.right));
-      o[14] = 0.0f;
-      o[15] = 0.0f;
+    out.stack_need = maxdepth + 1;
+    out.inner.resize(16 * kept.size());
+    parallel_for(kept.size(), [&](size_t b, size_t e, unsigned) {
+      for (size_t i = b; i < e; ++i) {
+        const RtBVHNode40& nd = nodes[kept[i]];
+        const RtBVHNode40& L = nodes[nd.left];
+        const RtBVHNode40& R = nodes[nd.right];
+        float* o = &out.inner[16 * i];
+        o[0] = L.minX; o[1] = L.maxX; o[2] = L.minY; o[3] = L.maxY;
+        o[4] = R.minX; o[5] = R.maxX; o[6] = R.minY; o[7] = R.maxY;
+        o[8] = L.minZ; o[9] = L.maxZ; o[10] = R.minZ; o[11] = R.maxZ;
+        o[12] = bits_f(ref_of(nd.left, dev));
+        o[13] = bits_f(ref_of(nd.right, dev));
+        o[14] = 0.0f;
+        o[15] = 0.0f;
+      }
+    });
+  } else {
+    // 4-wide device tree: each wide node takes a binary node's two children
+    // and splits the child with the largest surface area until it has four,
+    // keeping left-to-right order (so leaf slots stay contiguous per subtree).
+    struct Wide {
+      uint32_t ch[4];
+      uint32_t count;
+    };
+    auto area = [&](uint32_t x) {
+      const RtBVHNode40& n = nodes[x];
+      const double dx = (double)n.maxX - n.minX, dy = (double)n.maxY - n.minY, dz = (double)n.maxZ - n.minZ;
+      return dx * dy + dy * dz + dz * dx;
+    };
+    std::vector<Wide> wn;
+    std::vector<uint32_t> todo{0u};
+    while (!todo.empty()) {
+      const uint32_t x = todo.back();
+      todo.pop_back();
+      Wide w;
+      w.ch[0] = nodes[x].left;
+      w.ch[1] = nodes[x].right;
+      w.count = 2;
+      while (w.count < 4) {
+        int best = -1;
+        double ba = -1.0;
+        for (uint32_t j = 0; j < w.count; ++j)
+          if (expandable(w.ch[j])) {
+            const double a = area(w.ch[j]);
+            if (a > ba) { ba = a; best = (int)j; }
+          }
+        if (best < 0) break;
+        const uint32_t c = w.ch[best];
+        for (uint32_t j = w.count; j > (uint32_t)best + 1; --j) w.ch[j] = w.ch[j - 1];
+        w.ch[best] = nodes[c].left;
+        w.ch[best + 1] = nodes[c].right;
+        w.count++;
+      }
+      dev[x] = (uint32_t)wn.size();
+      wn.push_back(w);
+      for (int j = (int)w.count - 1; j >= 0; --j)
+        if (expandable(w.ch[j])) todo.push_back(w.ch[j]);
     }
-  });
+    // depth and worst-case stack use (a visit pushes at most count-1 entries)
+    std::vector<uint32_t> need(wn.size()), dep(wn.size());
+    for (size_t k = wn.size(); k-- > 0;) {
+      uint32_t nd = 0, dd = 0;
+      for (uint32_t j = 0; j < wn[k].count; ++j)
+        if (expandable(wn[k].ch[j])) {
+          nd = std::max(nd, need[dev[wn[k].ch[j]]]);
+          dd = std::max(dd, dep[dev[wn[k].ch[j]]]);
+        }
+      need[k] = nd + wn[k].count - 1u;
+      dep[k] = dd + 1u;
+    }
+    out.root = 0;
+    out.depth = dep[0];
+    out.stack_need = need[0] + 1u;
+    // Quantised child boxes: node origin p = min of the child boxes; per axis a
+    // power-of-two step s = 2^e with 255*s >= extent; child bounds rounded
+    // outward to multiples of s, so p + q*s encloses every child box.
+    out.inner.resize(16 * wn.size());
+    parallel_for(wn.size(), [&](size_t b, size_t e, unsigned) {
+      for (size_t i = b; i < e; ++i) {
+        const Wide& w = wn[i];
+        float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+        for (uint32_t j = 0; j < w.count; ++j) {
+          const RtBVHNode40& c = nodes[w.ch[j]];
+          const float cl[3] = {c.minX, c.minY, c.minZ}, chh[3] = {c.maxX, c.maxY, c.maxZ};
+          for (int a = 0; a < 3; ++a) {
+            lo[a] = std::fmin(lo[a], cl[a]);
+            hi[a] = std::fmax(hi[a], chh[a]);
+          }
+        }
+        int ex[3];
+        for (int a = 0; a < 3; ++a) {
+          const double ext = (double)hi[a] - (double)lo[a];
+          int e2 = -126;
+          if (ext > 0.0) {
+            e2 = (int)std::ceil(std::log2(ext / 255.0));
+            while (255.0 * std::ldexp(1.0, e2) < ext) ++e2;
+            while (e2 > -126 && 255.0 * std::ldexp(1.0, e2 - 1) >= ext) --e2;
+          }
+          ex[a] = std::max(-126, std::min(127, e2));
+        }
+        uint32_t q[6] = {0, 0, 0, 0, 0, 0};  // qlo_x, qhi_x, qlo_y, qhi_y, qlo_z, qhi_z
+        for (uint32_t j = w.count; j < 4; ++j)  // unused slot: qlo 255 > qhi 0, empty for any ray
+          for (int a = 0; a < 3; ++a) q[2 * a] |= 255u << (8 * j);
+        for (uint32_t j = 0; j < w.count; ++j) {
+          const RtBVHNode40& c = nodes[w.ch[j]];
+          const float cl[3] = {c.minX, c.minY, c.minZ}, chh[3] = {c.maxX, c.maxY, c.maxZ};
+          for (int a = 0; a < 3; ++a) {
+            const double st = std::ldexp(1.0, ex[a]);
+            double ql = std::floor(((double)cl[a] - (double)lo[a]) / st);
+            double qh = std::ceil(((double)chh[a] - (double)lo[a]) / st);
+            ql = std::min(255.0, std::max(0.0, ql));
+            qh = std::min(255.0, std::max(0.0, qh));
+            q[2 * a] |= (uint32_t)ql << (8 * j);
+            q[2 * a + 1] |= (uint32_t)qh << (8 * j);
+          }
+        }
+        float* o = &out.inner[16 * i];
+        o[0] = lo[0]; o[1] = lo[1]; o[2] = lo[2];
+        o[3] = bits_f((uint32_t)(ex[0] + 127) | ((uint32_t)(ex[1] + 127) << 8) | ((uint32_t)(ex[2] + 127) << 16) |
+                      (w.count << 24));
+        for (uint32_t j = 0; j < 4; ++j)
+          o[4 + j] = bits_f(j < w.count ? ref_of(w.ch[j], dev) : (kLeafBit | kSphereBit | kSphereMask));
+        for (int k = 0; k < 6; ++k) o[8 + k] = bits_f(q[k]);
+        o[14] = 0.0f;
+        o[15] = 0.0f;
+      }
+    });
+  }
 
   // Triangle records in slot order.
   out.tris.resize(16 * (size_t)nslots);

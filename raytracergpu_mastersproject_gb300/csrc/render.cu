@@ -8,6 +8,8 @@
 // and written once.  Persistent warps take 32 pixels at a time from a counter.
 #include <cuda_runtime.h>
 
+#include <type_traits>
+
 #include "trace_core.cuh"
 
 namespace rtgb {
@@ -80,17 +82,21 @@ __device__ __forceinline__ f3 random_unit_vector(uint32_t& rng) {
   return normalize(mk(rho * sp * ct, rho * sp * st, rho * cp));
 }
 
-template <int STACK>
+template <int W, int STACK, typename StackT>
 __device__ f3 ray_color(const DeviceScene& S, f3 o, f3 d, uint32_t depth, uint32_t& rng, bool extended, f3 bg,
-                        uint32_t* stack, uint32_t& status) {
+                        StackT* stack, uint32_t& status) {
   f3 color = mk(0.0f, 0.0f, 0.0f);
   f3 gatt = mk(1.0f, 1.0f, 1.0f);
   f3 co = o, cd = normalize(d);
   for (uint32_t i = 0; i < depth; ++i) {
     dev::Trav s;
-    dev::trav_init(s, make_float4(co.x, co.y, co.z, 0.001f), make_float4(cd.x, cd.y, cd.z, 10000000.0f), S.root,
-                   stack);
-    dev::trav_run<false, STACK>(S, s, stack, 0);
+    dev::trav_init_ray(s, make_float4(co.x, co.y, co.z, 0.001f), make_float4(cd.x, cd.y, cd.z, 10000000.0f), S.root);
+    if constexpr (W == 2) {
+      stack[0] = kSentinel;
+      dev::trav_run<false, STACK>(S, s, stack, 0);
+    } else {
+      dev::trav_run_wide<false, STACK>(S, s, stack, 0);
+    }
     if (s.sp < 0) status |= 1u;
     if (s.best == dev::kNoBest || s.sp < 0) {
       const f3 b = extended ? bg : mk(0.0f, 0.0f, 0.0f);
@@ -170,13 +176,14 @@ __device__ __forceinline__ uint32_t lanemask_lt() {
   return m;
 }
 
-template <int STACK>
+template <int W, int STACK>
 __global__ void __launch_bounds__(kThreads) k_render(DeviceScene S, Cam cam, uint32_t depth, uint32_t random_state,
-                                                     float4* __restrict__ accum, uint32_t W, uint32_t H, uint32_t spp,
+                                                     float4* __restrict__ accum, uint32_t Wd, uint32_t H, uint32_t spp,
                                                      uint32_t extended, float bgx, float bgy, float bgz,
                                                      uint32_t* __restrict__ counter) {
-  uint32_t stack[STACK];
-  const uint32_t total = W * H;
+  using StackT = typename std::conditional<W == 2, uint32_t, uint2>::type;
+  StackT stack[STACK];
+  const uint32_t total = Wd * H;
   const uint32_t lane = threadIdx.x & 31u;
   const f3 pos = mk(cam.v[0], cam.v[1], cam.v[2]);
   const f3 p00 = mk(cam.v[3], cam.v[4], cam.v[5]);
@@ -191,7 +198,7 @@ __global__ void __launch_bounds__(kThreads) k_render(DeviceScene S, Cam cam, uin
     if (base >= total) break;
     const uint32_t i = base + lane;
     if (i < total) {
-      const uint32_t x = i % W, y = i / W;
+      const uint32_t x = i % Wd, y = i / Wd;
       float4 px = accum[i];
       for (uint32_t smp = 0; smp < spp; ++smp) {
         uint32_t rng = (600u * x + y) * (random_state + 1u);  // random.glsl:9
@@ -199,7 +206,7 @@ __global__ void __launch_bounds__(kThreads) k_render(DeviceScene S, Cam cam, uin
         const float next = rng_next(rng);                     // :352 (:351 is a no-op)
         const f3 sample = add(add(p00, scale(pdu, (float)x)), scale(pdv, (float)y));
         const f3 d = normalize(sub(sample, pos));
-        const f3 c = ray_color<STACK>(S, pos, d, depth, rng, extended != 0u, bg, stack, status);
+        const f3 c = ray_color<W, STACK>(S, pos, d, depth, rng, extended != 0u, bg, stack, status);
         px.x = c.x + px.x;
         px.y = c.y + px.y;
         px.z = c.z + px.z;
@@ -229,13 +236,13 @@ __global__ void k_resolve(const float4* accum, uint32_t total, float inv_spp_den
   }
 }
 
-template <int STACK>
+template <int W, int STACK>
 cudaError_t launch_render_variant(const DeviceScene& S, const Cam& cam, uint32_t depth, uint32_t rs, float* accum,
                                   uint32_t w, uint32_t h, uint32_t spp, uint32_t shade, const float bg[3],
                                   uint32_t* counter, cudaStream_t st) {
   static int blocks_per_sm = -1;
   if (blocks_per_sm < 0) {
-    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, k_render<STACK>, kThreads, 0);
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, k_render<W, STACK>, kThreads, 0);
     if (e != cudaSuccess) return e;
     if (blocks_per_sm < 1) blocks_per_sm = 1;
   }
@@ -244,7 +251,7 @@ cudaError_t launch_render_variant(const DeviceScene& S, const Cam& cam, uint32_t
   const uint32_t needed = (total + kThreads - 1) / kThreads;
   if (blocks > needed) blocks = needed;
   if (blocks == 0) blocks = 1;
-  k_render<STACK><<<blocks, kThreads, 0, st>>>(S, cam, depth, rs, reinterpret_cast<float4*>(accum), w, h, spp,
+  k_render<W, STACK><<<blocks, kThreads, 0, st>>>(S, cam, depth, rs, reinterpret_cast<float4*>(accum), w, h, spp,
                                                shade == RT_SHADE_EXTENDED ? 1u : 0u, bg[0], bg[1], bg[2], counter);
   return cudaGetLastError();
 }
@@ -257,8 +264,14 @@ cudaError_t launch_render(const DeviceScene& s, const float cam[12], uint32_t de
   Cam c;
   for (int k = 0; k < 12; ++k) c.v[k] = cam[k];
   cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
-  if (s.depth < 64u) return launch_render_variant<64>(s, c, depth, random_state, accum, w, h, spp, shade_mode, bg, counter, st);
-  return launch_render_variant<128>(s, c, depth, random_state, accum, w, h, spp, shade_mode, bg, counter, st);
+  if (s.width == 4) {
+    if (s.stack_need <= 64u)
+      return launch_render_variant<4, 64>(s, c, depth, random_state, accum, w, h, spp, shade_mode, bg, counter, st);
+    return launch_render_variant<4, 192>(s, c, depth, random_state, accum, w, h, spp, shade_mode, bg, counter, st);
+  }
+  if (s.stack_need <= 64u)
+    return launch_render_variant<2, 64>(s, c, depth, random_state, accum, w, h, spp, shade_mode, bg, counter, st);
+  return launch_render_variant<2, 128>(s, c, depth, random_state, accum, w, h, spp, shade_mode, bg, counter, st);
 }
 
 cudaError_t launch_accum_clear(float* accum, uint32_t w, uint32_t h, void* stream) {

@@ -49,6 +49,7 @@ constexpr uint32_t kMaxLeafSize = 8;
 constexpr uint32_t kMaxTriangles = 1u << 27;
 constexpr uint32_t kSentinel = 0x7FFFFFFFu;  // stack bottom, never a node index
 constexpr uint32_t kDefaultLeafSize = 1;
+constexpr uint32_t kDefaultWidth = 4;
 
 struct DeviceScene {
   const void* inner = nullptr;     // float4[4 * n_inner]
@@ -63,6 +64,8 @@ struct DeviceScene {
   uint32_t n_spheres = 0;
   uint32_t n_mats = 0;
   uint32_t depth = 0;
+  uint32_t width = 2;       // 2: binary child-box nodes; 4: quantised 4-wide nodes
+  uint32_t stack_need = 0;  // worst-case traversal stack entries
 };
 
 // Host-side result of the BVH conversion, ready to upload.
@@ -75,6 +78,8 @@ struct HostDeviceBVH {
   std::vector<float> mats;         // 8 floats per material
   uint32_t root = kSentinel;
   uint32_t depth = 0;
+  uint32_t width = 2;
+  uint32_t stack_need = 1;
 };
 
 // ---- host BVH builder (host_bvh.cpp) ----
@@ -89,7 +94,7 @@ void build_bvh(const RtTriangle64* tris, uint32_t nt, const RtSphere32* sph, uin
 // Validates a reference-layout tree and converts it to the device form.
 bool convert_bvh(const RtBVHNode40* nodes, uint32_t nn, const RtTriangle64* tris, uint32_t nt,
                  const RtSphere32* sph, uint32_t ns, const RtMaterial32* mats, uint32_t nm,
-                 uint32_t leaf_size, HostDeviceBVH& out, std::string& msg);
+                 uint32_t leaf_size, uint32_t width, HostDeviceBVH& out, std::string& msg);
 // Camera of raytraceBVH.comp:50-81: out = camPos, pixel00, pixelDeltaU, pixelDeltaV.
 void camera_setup(const RtRaytraceUBO& ubo, uint32_t width, uint32_t height, float out[12]);
 
@@ -121,6 +126,20 @@ struct LaunchCfg {
   int blocks = 0;
   int threads = 0;
 };
+// Launch shape of the ray-query kernel: variant = (threads per block, min
+// resident blocks) pair from a fixed table, refill threshold, grid size in
+// percent of the resident-block count.
+struct TraceTuning {
+  int variant = 0;
+  int refill = 20;
+  int grid_scale = 100;
+};
+TraceTuning default_tuning();
+int num_trace_variants();
+void trace_variant_shape(int v, int* threads, int* minb);
+cudaError_t launch_trace_tuned(const DeviceScene& s, const RtRay* rays, uint32_t n, RtHit* hits, uint32_t flags,
+                               uint32_t* counter, void* stream, const TraceTuning& tune,
+                               unsigned long long* stats);
 // Kernels launch on the given stream; counter is a device uint32 zeroed by the caller.
 cudaError_t launch_trace(const DeviceScene& s, const RtRay* rays, uint32_t n, RtHit* hits, uint32_t flags,
                          uint32_t* counter, void* stream);

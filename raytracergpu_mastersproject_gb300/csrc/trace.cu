@@ -1,12 +1,18 @@
 // trace.cu -- ray-query kernels (closest hit / any hit) for sm_103a.
 //
 // Replaces hitBVH/sceneHit (raytraceBVH.comp:195-274) for batches of
-// independent rays.  Persistent warps: each warp takes rays 32 at a time from
-// a global counter (one atomicAdd per refill), traverses them with the
-// near-first while-while loop of trace_core.cuh, and hands new rays to lanes
-// that finished whenever fewer than kRefill lanes are still busy.
+// independent rays.  Persistent warps take rays from a global counter (one
+// atomicAdd per refill, indices handed out with __ballot_sync/__popc/
+// __shfl_sync).  Two loop shapes:
+//   k_trace       near-first while-while loop with postponed leaves (binary
+//                 and 4-wide trees); idle lanes are refilled when fewer than
+//                 `refill` lanes still traverse.
+//   k_trace_step  4-wide trees: one traversal step per lane per iteration and
+//                 refill as soon as `refill` lanes are idle (the default).
 #include <cuda_runtime.h>
 
+#include <cstdlib>
+#include <type_traits>
 #include <mutex>
 
 #include "trace_core.cuh"
@@ -14,23 +20,26 @@
 namespace rtgb {
 namespace {
 
-constexpr int kThreads = 128;
-constexpr int kRefill = 20;
-
 __device__ __forceinline__ uint32_t lanemask_lt() {
   uint32_t m;
   asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
   return m;
 }
 
-template <bool ANY, int STACK>
-__global__ void __launch_bounds__(kThreads) k_trace(DeviceScene S, const float4* __restrict__ rays, uint32_t n,
-                                                    uint2* __restrict__ hits, uint32_t* __restrict__ counter) {
-  uint32_t stack[STACK];
+// THREADS per block and MINB resident blocks per SM (the register cap) are
+// launch-shape knobs; `refill` is the lane count below which a warp stops to
+// hand new rays to its idle lanes (0: only when all lanes are idle).
+template <bool ANY, int STACK, int THREADS, int MINB, int W, bool STATS>
+__global__ void __launch_bounds__(THREADS, MINB)
+    k_trace(DeviceScene S, const float4* __restrict__ rays, uint32_t n, uint2* __restrict__ hits,
+            uint32_t* __restrict__ counter, int refill, unsigned long long* __restrict__ stats) {
+  using StackT = typename std::conditional<W == 2, uint32_t, uint2>::type;
+  StackT stack[STACK];
   dev::Trav s;
   const uint32_t lane = threadIdx.x & 31u;
   uint32_t ray = 0xFFFFFFFFu;
   bool exhausted = false;
+  unsigned long long vis = 0, tests = 0;
   for (;;) {
     const bool idle = ray == 0xFFFFFFFFu;
     const uint32_t m = __ballot_sync(0xFFFFFFFFu, idle);
@@ -43,13 +52,18 @@ __global__ void __launch_bounds__(kThreads) k_trace(DeviceScene S, const float4*
         const uint32_t id = base + (uint32_t)__popc(m & lanemask_lt());
         if (id < n) {
           ray = id;
-          dev::trav_init(s, __ldg(&rays[2u * id]), __ldg(&rays[2u * id + 1u]), S.root, stack);
+          dev::trav_init_ray(s, __ldg(&rays[2u * id]), __ldg(&rays[2u * id + 1u]), S.root);
+          if constexpr (W == 2) stack[0] = kSentinel;
         }
       }
     }
     if (__all_sync(0xFFFFFFFFu, ray == 0xFFFFFFFFu)) break;
     if (ray != 0xFFFFFFFFu) {
-      const bool done = dev::trav_run<ANY, STACK>(S, s, stack, exhausted ? 0 : kRefill);
+      bool done;
+      if constexpr (W == 2)
+        done = dev::trav_run<ANY, STACK>(S, s, stack, exhausted ? 0 : refill);
+      else
+        done = dev::trav_run_wide<ANY, STACK>(S, s, stack, exhausted ? 0 : refill);
       if (done || s.sp < 0) {
         uint2 h;
         if (s.sp < 0 || s.best == dev::kNoBest) {
@@ -63,32 +77,207 @@ __global__ void __launch_bounds__(kThreads) k_trace(DeviceScene S, const float4*
           h.y = __float_as_uint(s.tclose);
         }
         hits[ray] = h;
+        if constexpr (STATS) {
+          vis += s.nvis;
+          tests += s.ntest;
+        }
         ray = 0xFFFFFFFFu;
       }
     }
   }
+  if constexpr (STATS) {
+    for (int o = 16; o > 0; o >>= 1) {
+      vis += __shfl_down_sync(0xFFFFFFFFu, vis, o);
+      tests += __shfl_down_sync(0xFFFFFFFFu, tests, o);
+    }
+    if (lane == 0) {
+      atomicAdd(&stats[0], vis);
+      atomicAdd(&stats[1], tests);
+    }
+  }
 }
 
-template <bool ANY, int STACK>
-cudaError_t launch_variant(const DeviceScene& S, const RtRay* rays, uint32_t n, RtHit* hits, uint32_t* counter,
-                           cudaStream_t st) {
-  static int blocks_per_sm = -1;
-  if (blocks_per_sm < 0) {
-    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, k_trace<ANY, STACK>, kThreads, 0);
-    if (e != cudaSuccess) return e;
-    if (blocks_per_sm < 1) blocks_per_sm = 1;
+// Per-step variant for 4-wide trees: every iteration each lane advances its
+// ray by exactly one step -- one inner node, or one leaf -- and lanes whose ray
+// finished take new rays as soon as `refill` of them are idle.  The heavy
+// inner-node step then runs with nearly all lanes active; leaves are rare.
+template <bool ANY, int STACK, int THREADS, int MINB, bool STATS>
+__global__ void __launch_bounds__(THREADS, MINB)
+    k_trace_step(DeviceScene S, const float4* __restrict__ rays, uint32_t n, uint2* __restrict__ hits,
+                 uint32_t* __restrict__ counter, int refill, unsigned long long* __restrict__ stats) {
+  uint2 stack[STACK];
+  dev::Trav s;
+  const uint32_t lane = threadIdx.x & 31u;
+  uint32_t ray = 0xFFFFFFFFu;
+  bool exhausted = false;
+  unsigned long long vis = 0, tests = 0;
+  const int min_idle = refill < 1 ? 1 : (refill > 32 ? 32 : refill);
+  for (;;) {
+    const uint32_t idle = __ballot_sync(0xFFFFFFFFu, ray == 0xFFFFFFFFu);
+    if (exhausted && idle == 0xFFFFFFFFu) break;
+    if (!exhausted && __popc(idle) >= min_idle) {
+      uint32_t base = 0;
+      if (lane == 0) base = atomicAdd(counter, (uint32_t)__popc(idle));
+      base = __shfl_sync(0xFFFFFFFFu, base, 0);
+      if (base + (uint32_t)__popc(idle) >= n) exhausted = true;
+      if (ray == 0xFFFFFFFFu) {
+        const uint32_t id = base + (uint32_t)__popc(idle & lanemask_lt());
+        if (id < n) {
+          ray = id;
+          dev::trav_init_ray(s, __ldg(&rays[2u * id]), __ldg(&rays[2u * id + 1u]), S.root);
+          if (s.leaf != 0u) {  // the whole tree is one leaf
+            s.node = s.leaf;
+            s.leaf = 0u;
+          }
+        }
+      }
+    }
+    if (ray == 0xFFFFFFFFu) continue;
+    bool done = false;
+    if (dev::is_inner(s.node)) {
+      if (!dev::visit_wide<STACK>(S, s, stack)) done = true;
+    } else if (dev::is_leaf(s.node)) {
+      if (dev::leaf_visit<ANY>(S, s, s.node))
+        done = true;
+      else
+        s.node = dev::pop_wide(s, stack);
+    }
+    if (done || s.node == kSentinel) {
+      uint2 h;
+      if (s.sp < 0 || s.best == dev::kNoBest) {
+        h.x = RT_NO_HIT;
+        h.y = __float_as_uint(__int_as_float(0x7f800000));
+      } else if (s.best & kSphereBit) {
+        h.x = (s.best & kSphereMask) | RT_HIT_SPHERE_BIT;
+        h.y = __float_as_uint(s.tclose);
+      } else {
+        h.x = __ldg(&S.tri_ids[s.best & kSlotMask]);
+        h.y = __float_as_uint(s.tclose);
+      }
+      hits[ray] = h;
+      if constexpr (STATS) {
+        vis += s.nvis;
+        tests += s.ntest;
+      }
+      ray = 0xFFFFFFFFu;
+    }
   }
-  const uint32_t warps_needed = (n + 31u) / 32u;
-  uint32_t blocks = (uint32_t)(device_sm_count() * blocks_per_sm);
-  const uint32_t blocks_needed = (warps_needed + (kThreads / 32) - 1) / (kThreads / 32);
-  if (blocks > blocks_needed) blocks = blocks_needed;
-  if (blocks == 0) blocks = 1;
-  k_trace<ANY, STACK><<<blocks, kThreads, 0, st>>>(S, reinterpret_cast<const float4*>(rays), n,
-                                                   reinterpret_cast<uint2*>(hits), counter);
-  return cudaGetLastError();
+  if constexpr (STATS) {
+    for (int o = 16; o > 0; o >>= 1) {
+      vis += __shfl_down_sync(0xFFFFFFFFu, vis, o);
+      tests += __shfl_down_sync(0xFFFFFFFFu, tests, o);
+    }
+    if (lane == 0) {
+      atomicAdd(&stats[0], vis);
+      atomicAdd(&stats[1], tests);
+    }
+  }
+}
+
+using TraceKernel = void (*)(DeviceScene, const float4*, uint32_t, uint2*, uint32_t*, int, unsigned long long*);
+
+// Stack capacities: binary trees 64 or 128 refs (depth + sentinel); 4-wide
+// trees 64 or 192 (ref, t) entries (worst-case pushes along a path).
+struct Variant {
+  int threads, minb;
+  TraceKernel k[2][2][2][2];  // [stats][wide][any][big stack]
+  int blocks_per_sm[2][2][2][2];
+};
+
+template <int T, int M, bool ST>
+void fill_variant(Variant& v) {
+  v.k[ST][0][0][0] = k_trace<false, 64, T, M, 2, ST>;
+  v.k[ST][0][0][1] = k_trace<false, 128, T, M, 2, ST>;
+  v.k[ST][0][1][0] = k_trace<true, 64, T, M, 2, ST>;
+  v.k[ST][0][1][1] = k_trace<true, 128, T, M, 2, ST>;
+  v.k[ST][1][0][0] = k_trace<false, 64, T, M, 4, ST>;
+  v.k[ST][1][0][1] = k_trace<false, 192, T, M, 4, ST>;
+  v.k[ST][1][1][0] = k_trace<true, 64, T, M, 4, ST>;
+  v.k[ST][1][1][1] = k_trace<true, 192, T, M, 4, ST>;
+}
+
+template <int T, int M, bool ST>
+void fill_step_variant(Variant& v) {
+  fill_variant<T, M, ST>(v);  // binary trees keep the while-while loop
+  v.k[ST][1][0][0] = k_trace_step<false, 64, T, M, ST>;
+  v.k[ST][1][0][1] = k_trace_step<false, 192, T, M, ST>;
+  v.k[ST][1][1][0] = k_trace_step<true, 64, T, M, ST>;
+  v.k[ST][1][1][1] = k_trace_step<true, 192, T, M, ST>;
+}
+
+template <int T, int M, bool STEP>
+Variant make_variant() {
+  Variant v;
+  v.threads = T;
+  v.minb = M;
+  if constexpr (STEP) {
+    fill_step_variant<T, M, false>(v);
+    fill_step_variant<T, M, true>(v);
+  } else {
+    fill_variant<T, M, false>(v);
+    fill_variant<T, M, true>(v);
+  }
+  for (auto& a : v.blocks_per_sm)
+    for (auto& b : a)
+      for (auto& c : b)
+        for (int& d : c) d = -1;
+  return v;
+}
+
+Variant g_variants[] = {make_variant<128, 12, false>(), make_variant<128, 10, false>(), make_variant<128, 1, false>(),
+                        make_variant<128, 12, true>(),  make_variant<128, 10, true>(),  make_variant<128, 1, true>()};
+constexpr int kNumVariants = sizeof(g_variants) / sizeof(g_variants[0]);
+
+int env_int(const char* name, int dflt) {
+  const char* e = std::getenv(name);
+  return e ? std::atoi(e) : dflt;
 }
 
 }  // namespace
+
+TraceTuning default_tuning() {
+  static TraceTuning t = [] {
+    TraceTuning d;
+    d.variant = env_int("RT_TRACE_VARIANT", 3);
+    d.refill = env_int("RT_TRACE_REFILL", 4);
+    d.grid_scale = env_int("RT_TRACE_GRID_PCT", 100);
+    return d;
+  }();
+  return t;
+}
+
+int num_trace_variants() { return kNumVariants; }
+void trace_variant_shape(int v, int* threads, int* minb) {
+  *threads = g_variants[v].threads;
+  *minb = g_variants[v].minb;
+}
+
+cudaError_t launch_trace_tuned(const DeviceScene& S, const RtRay* rays, uint32_t n, RtHit* hits, uint32_t flags,
+                               uint32_t* counter, void* stream, const TraceTuning& tune, unsigned long long* stats) {
+  const int vi = (tune.variant >= 0 && tune.variant < kNumVariants) ? tune.variant : 0;
+  Variant& v = g_variants[vi];
+  const int any = (flags & RT_TRACE_ANY) != 0 ? 1 : 0;
+  const int wide = S.width == 4 ? 1 : 0;
+  const int big = S.stack_need > 64u ? 1 : 0;
+  const int st = stats ? 1 : 0;
+  TraceKernel k = v.k[st][wide][any][big];
+  int& bps = v.blocks_per_sm[st][wide][any][big];
+  if (bps < 0) {
+    int b = 0;
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k, v.threads, 0);
+    if (e != cudaSuccess) return e;
+    bps = b < 1 ? 1 : b;
+  }
+  const uint32_t warps_per_block = (uint32_t)v.threads / 32u;
+  const uint32_t warps_needed = (n + 31u) / 32u;
+  uint64_t blocks = (uint64_t)device_sm_count() * (uint64_t)bps * (uint64_t)std::max(1, tune.grid_scale) / 100u;
+  const uint64_t needed = (warps_needed + warps_per_block - 1) / warps_per_block;
+  if (blocks > needed) blocks = needed;
+  if (blocks == 0) blocks = 1;
+  k<<<(uint32_t)blocks, v.threads, 0, reinterpret_cast<cudaStream_t>(stream)>>>(
+      S, reinterpret_cast<const float4*>(rays), n, reinterpret_cast<uint2*>(hits), counter, tune.refill, stats);
+  return cudaGetLastError();
+}
 
 int device_sm_count() {
   static int sms = -1;
@@ -102,14 +291,7 @@ int device_sm_count() {
 
 cudaError_t launch_trace(const DeviceScene& s, const RtRay* rays, uint32_t n, RtHit* hits, uint32_t flags,
                          uint32_t* counter, void* stream) {
-  cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
-  const bool any = (flags & RT_TRACE_ANY) != 0;
-  if (s.depth < 64u) {
-    return any ? launch_variant<true, 64>(s, rays, n, hits, counter, st)
-               : launch_variant<false, 64>(s, rays, n, hits, counter, st);
-  }
-  return any ? launch_variant<true, 128>(s, rays, n, hits, counter, st)
-             : launch_variant<false, 128>(s, rays, n, hits, counter, st);
+  return launch_trace_tuned(s, rays, n, hits, flags, counter, stream, default_tuning(), nullptr);
 }
 
 // ---- allocation-free ray queries (rt_trace_noalloc) ----

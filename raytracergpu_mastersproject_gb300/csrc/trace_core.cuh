@@ -83,6 +83,7 @@ struct Trav {
   uint32_t node;                 // next node to visit, or a leaf, or kSentinel
   uint32_t leaf;                 // postponed leaf (0: none)
   int sp;                        // stack top index; stack[0] = kSentinel
+  uint32_t nvis, ntest;          // inner nodes fetched, primitives tested
 };
 
 // Box culling margin: wider than the binary32 rounding of box and triangle
@@ -96,8 +97,8 @@ __device__ __forceinline__ void trav_set_close(Trav& s, float t) {
   s.cull_hi = fmaf(fabsf(t), kCullRel, t);
 }
 
-__device__ __forceinline__ void trav_init(Trav& s, const float4 o_tmin, const float4 d_tmax, uint32_t root,
-                                          uint32_t* stack) {
+// Loads one ray into the state; the caller prepares its stack.
+__device__ __forceinline__ void trav_init_ray(Trav& s, const float4 o_tmin, const float4 d_tmax, uint32_t root) {
   s.ox = o_tmin.x; s.oy = o_tmin.y; s.oz = o_tmin.z; s.tmin = o_tmin.w;
   s.dx = d_tmax.x; s.dy = d_tmax.y; s.dz = d_tmax.z;
   const float eps = 1e-30f;
@@ -114,6 +115,14 @@ __device__ __forceinline__ void trav_init(Trav& s, const float4 o_tmin, const fl
     s.node = kSentinel;
   }
   s.sp = 0;
+  s.nvis = 0;
+  s.ntest = 0;
+}
+
+// Binary-tree stack: stack[0] holds the sentinel, sp is the top index.
+__device__ __forceinline__ void trav_init(Trav& s, const float4 o_tmin, const float4 d_tmax, uint32_t root,
+                                          uint32_t* stack) {
+  trav_init_ray(s, o_tmin, d_tmax, root);
   stack[0] = kSentinel;
 }
 
@@ -139,6 +148,7 @@ __device__ __forceinline__ bool leaf_visit(const DeviceScene& S, Trav& s, uint32
   if (leaf & kSphereBit) {
     const uint32_t idx = leaf & kSphereMask;
     float t;
+    s.ntest++;
     if (idx < S.n_spheres && sphere_test(S.spheres, idx, s.ox, s.oy, s.oz, s.dx, s.dy, s.dz, s.tmin, s.tclose, t)) {
       trav_set_close(s, t);
       s.best = leaf;
@@ -150,6 +160,7 @@ __device__ __forceinline__ bool leaf_visit(const DeviceScene& S, Trav& s, uint32
   const uint32_t count = ((leaf >> kCountShift) & 7u) + 1u;
   for (uint32_t k = 0; k < count; ++k) {
     float t;
+    s.ntest++;
     if (tri_test(S.tris, first + k, s.ox, s.oy, s.oz, s.dx, s.dy, s.dz, s.tmin, s.tclose, t)) {
       trav_set_close(s, t);
       s.best = kLeafBit | (first + k);
@@ -168,6 +179,7 @@ __device__ __forceinline__ bool trav_run(const DeviceScene& S, Trav& s, uint32_t
   for (;;) {
     // Inner nodes: descend, postponing the first leaf found.
     while (is_inner(s.node)) {
+      s.nvis++;
       const float4 a = ldg4(S.inner, 4u * s.node + 0u);
       const float4 b = ldg4(S.inner, 4u * s.node + 1u);
       const float4 c = ldg4(S.inner, 4u * s.node + 2u);
@@ -216,6 +228,139 @@ __device__ __forceinline__ bool trav_run(const DeviceScene& S, Trav& s, uint32_t
         s.leaf = s.node;
         s.node = stack[s.sp];
         s.sp = s.sp > 0 ? s.sp - 1 : 0;
+      }
+    }
+    if (s.node == kSentinel) return true;
+    if (refill > 0 && __popc(__activemask()) < refill) return false;
+  }
+}
+
+// ------------------------------------------------------ 4-wide nodes ----
+// Node (64 B): float4 (p.xyz, meta), uint4 refs, uint4 (qlo_x, qhi_x, qlo_y,
+// qhi_y), uint4 (qlo_z, qhi_z, -, -); meta = exponent bytes ex|ey<<8|ez<<16
+// (biased by 127) | child count << 24.  Child i spans p + q*2^e per axis,
+// with q the i-th byte of the matching word.
+//
+// A plane's parameter is fma(q, A, B) with A = 2^e/d (exact) and
+// B = (p - o)/d.  Against the exact value it is off by less than
+// 2 ulp of |t| plus 5 ulp of |B| (one rounding each for 1/d, p - o, the
+// product, B -/+ e and the fma).  Each axis therefore uses B - e for its near
+// plane and B + e for its far plane, e = |B| * 2^-21 (8 ulp), and the
+// resulting interval is widened by |t| * 2^-21.  The near plane of an axis is
+// the low bound when d >= 0 and the high bound otherwise, so no per-axis
+// min/max is needed.
+constexpr float kWideWidenB = 4.76837158203125e-07f;  // 2^-21
+
+// Stack entries are (ref, t_near); an entry that starts beyond the closest
+// hit is dropped when popped, without fetching it.  sp counts entries.
+__device__ __forceinline__ uint32_t pop_wide(Trav& s, const uint2* stack) {
+  while (s.sp > 0) {
+    const uint2 e = stack[--s.sp];
+    if (__uint_as_float(e.y) <= s.cull_hi) return e.x;
+  }
+  return kSentinel;
+}
+
+// Byte i of w as a float: the byte is placed under exponent 2^23 (0x4B000000)
+// and 2^23 subtracted, both exact.
+__device__ __forceinline__ float fmax3(float a, float b, float c) {
+  float d;
+  asm("max.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
+  return d;
+}
+__device__ __forceinline__ float fmin3(float a, float b, float c) {
+  float d;
+  asm("min.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
+  return d;
+}
+
+template <int I>
+__device__ __forceinline__ float qbyte(uint32_t w) {
+  return __uint_as_float(__byte_perm(w, 0x4B000000u, (uint32_t)I | 0x7650u)) - 8388608.0f;
+}
+
+// One 4-wide inner node: tests its children, pushes all hit children but the
+// nearest, and moves to the nearest (or pops).  Returns false on stack
+// overflow (s.sp = -1).
+template <int STACK>
+__device__ __forceinline__ bool visit_wide(const DeviceScene& S, Trav& s, uint2* stack) {
+  s.nvis++;
+  const float4 h = ldg4(S.inner, 4u * s.node + 0u);
+  const float4 r = ldg4(S.inner, 4u * s.node + 1u);
+  const float4 qa = ldg4(S.inner, 4u * s.node + 2u);
+  const float4 qb = ldg4(S.inner, 4u * s.node + 3u);
+  const uint32_t meta = fbits(h.w);
+  const float ax = __uint_as_float((meta & 0xFFu) << 23) * s.ix;
+  const float ay = __uint_as_float(((meta >> 8) & 0xFFu) << 23) * s.iy;
+  const float az = __uint_as_float(((meta >> 16) & 0xFFu) << 23) * s.iz;
+  const float bx = (h.x - s.ox) * s.ix, by = (h.y - s.oy) * s.iy, bz = (h.z - s.oz) * s.iz;
+  const float bxn = fmaf(-fabsf(bx), kWideWidenB, bx), bxf = fmaf(fabsf(bx), kWideWidenB, bx);
+  const float byn = fmaf(-fabsf(by), kWideWidenB, by), byf = fmaf(fabsf(by), kWideWidenB, by);
+  const float bzn = fmaf(-fabsf(bz), kWideWidenB, bz), bzf = fmaf(fabsf(bz), kWideWidenB, bz);
+  // near/far words per axis from the direction's sign; unused child slots
+  // hold qlo = 255 > qhi = 0, an empty interval for either sign.
+  const uint32_t nx = s.ix >= 0.0f ? fbits(qa.x) : fbits(qa.y), fx = s.ix >= 0.0f ? fbits(qa.y) : fbits(qa.x);
+  const uint32_t ny = s.iy >= 0.0f ? fbits(qa.z) : fbits(qa.w), fy = s.iy >= 0.0f ? fbits(qa.w) : fbits(qa.z);
+  const uint32_t nz = s.iz >= 0.0f ? fbits(qb.x) : fbits(qb.y), fz = s.iz >= 0.0f ? fbits(qb.y) : fbits(qb.x);
+  const float inf = __int_as_float(0x7f800000);
+  float t0, t1, t2, t3;
+  uint32_t r0 = fbits(r.x), r1 = fbits(r.y), r2 = fbits(r.z), r3 = fbits(r.w);
+#define RT_CHILD(I, T)                                                                            \
+  {                                                                                               \
+    float n = fmax3(fmaf(qbyte<I>(nx), ax, bxn), fmaf(qbyte<I>(ny), ay, byn), fmaf(qbyte<I>(nz), az, bzn)); \
+    float f = fmin3(fmaf(qbyte<I>(fx), ax, bxf), fmaf(qbyte<I>(fy), ay, byf), fmaf(qbyte<I>(fz), az, bzf)); \
+    n = fmaxf(fmaf(-fabsf(n), kSlabWiden, n), s.cull_lo);                                         \
+    f = fminf(fmaf(fabsf(f), kSlabWiden, f), s.cull_hi);                                          \
+    T = n <= f ? n : inf;                                                                         \
+  }
+  RT_CHILD(0, t0) RT_CHILD(1, t1) RT_CHILD(2, t2) RT_CHILD(3, t3)
+#undef RT_CHILD
+  // nearest child next; the others go on the stack, the runner-up last
+#define RT_SWAP(ta, ra, tb, rb)                       \
+  if (tb < ta) {                                      \
+    const float tt = ta; ta = tb; tb = tt;            \
+    const uint32_t rr = ra; ra = rb; rb = rr;         \
+  }
+  RT_SWAP(t0, r0, t1, r1) RT_SWAP(t2, r2, t3, r3) RT_SWAP(t0, r0, t2, r2)
+#undef RT_SWAP
+  // t0 is the minimum; t2 (the other pair's minimum) is pushed last
+  const int nh = (t0 < inf) + (t1 < inf) + (t2 < inf) + (t3 < inf);
+  if (nh == 0) {
+    s.node = pop_wide(s, stack);
+  } else {
+    if (s.sp + nh - 1 > STACK) {
+      s.sp = -1;
+      return false;
+    }
+    if (t3 < inf) stack[s.sp++] = make_uint2(r3, __float_as_uint(t3));
+    if (t1 < inf) stack[s.sp++] = make_uint2(r1, __float_as_uint(t1));
+    if (t2 < inf) stack[s.sp++] = make_uint2(r2, __float_as_uint(t2));
+    s.node = r0;
+  }
+  return true;
+}
+
+template <bool ANY, int STACK>
+__device__ __forceinline__ bool trav_run_wide(const DeviceScene& S, Trav& s, uint2* stack, int refill) {
+  for (;;) {
+    while (is_inner(s.node)) {
+      if (!visit_wide<STACK>(S, s, stack)) return false;
+      if (is_leaf(s.node) && s.leaf == 0u) {
+        s.leaf = s.node;
+        s.node = pop_wide(s, stack);
+      }
+      if (__all_sync(__activemask(), s.leaf != 0u)) break;
+    }
+    while (s.leaf != 0u) {
+      if (leaf_visit<ANY>(S, s, s.leaf)) {
+        s.leaf = 0u;
+        s.node = kSentinel;
+        return true;
+      }
+      s.leaf = 0u;
+      if (is_leaf(s.node)) {
+        s.leaf = s.node;
+        s.node = pop_wide(s, stack);
       }
     }
     if (s.node == kSentinel) return true;

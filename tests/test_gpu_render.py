@@ -42,12 +42,13 @@ def rmse(a, b):
     return float(np.sqrt(np.mean((a.astype(np.float64) - b.astype(np.float64)) ** 2)))
 
 
+@pytest.mark.parametrize("width", [2, 4])
 @pytest.mark.parametrize("mode", [0, 1], ids=["sorted", "reference"])
-def test_reference_shading(rt, orc, cuda, mode):
+def test_reference_shading(rt, orc, cuda, mode, width):
     tris, mats = lit_scene(rt)
     ubo = rt.make_ubo((0.0, 0.5, 4.0), (0.0, 0.0, 0.0), fov=60.0, depth=5, random_state=12345)
     w, h, spp = 96, 54, 4
-    with rt.Scene(tris, materials=mats, bvh_mode=mode) as sc:
+    with rt.Scene(tris, materials=mats, bvh_mode=mode, node_width=width) as sc:
         img = gpu_render(rt, cuda, sc, ubo, w, h, spp)
         ref = oracle_render(orc, tris, sc.nodes(), mats, ubo, w, h, spp)
     assert rmse(img, ref) <= 1e-3
@@ -66,7 +67,8 @@ def test_samples_split_across_calls(rt, cuda):
     assert np.array_equal(a, b)
 
 
-def test_extended_materials_and_spheres(rt, orc, cuda):
+@pytest.mark.parametrize("width", [2, 4])
+def test_extended_materials_and_spheres(rt, orc, cuda, width):
     tris, mats = rt.gen_spheres_scene(21, 6, 2, 0.05)
     ground = rt.gen_config1()[0][-2:].copy()
     ground["v0"][:, 1] = ground["v1"][:, 1] = ground["v2"][:, 1] = -9.0
@@ -87,7 +89,7 @@ def test_extended_materials_and_spheres(rt, orc, cuda):
     ubo = rt.make_ubo((0.0, 3.0, 28.0), (0.0, 0.0, 0.0), fov=40.0, depth=8, random_state=7)
     w, h, spp = 80, 45, 3
     bg = (0.6, 0.7, 1.0)
-    with rt.Scene(allt, spheres=sph, materials=allm) as sc:
+    with rt.Scene(allt, spheres=sph, materials=allm, node_width=width) as sc:
         img = gpu_render(rt, cuda, sc, ubo, w, h, spp, shade_mode=rt.SHADE_EXTENDED, background=bg)
         ref = oracle_render(orc, allt, sc.nodes(), allm, ubo, w, h, spp, spheres=sph, extended=True, background=bg)
         img_ref_mode = gpu_render(rt, cuda, sc, ubo, w, h, spp)

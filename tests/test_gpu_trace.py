@@ -31,10 +31,12 @@ def assert_parity(orc, tris, rays, ref, got):
     return arb
 
 
+@pytest.mark.parametrize("width", [2, 4])
 @pytest.mark.parametrize("mode", [0, 1], ids=["sorted", "reference"])
-def test_config1_matches_reference_order(rt, orc, cuda, mode):
+def test_config1_matches_reference_order(rt, orc, cuda, mode, width):
     tris, ubo, rays = rt.gen_config1()
-    with rt.Scene(tris, bvh_mode=mode) as sc:
+    with rt.Scene(tris, bvh_mode=mode, node_width=width) as sc:
+        assert sc.info().node_width == width
         got = dev_trace(rt, cuda, sc, rays)
         ref, st = orc.trace(orc.Scene(tris, sc.nodes()), rays)
     assert st[4] == 0
@@ -43,10 +45,11 @@ def test_config1_matches_reference_order(rt, orc, cuda, mode):
     assert arb["mismatch"] <= 20
 
 
+@pytest.mark.parametrize("width", [2, 4])
 @pytest.mark.parametrize("leaf", [2, 4, 8])
-def test_collapsed_leaves_same_hits(rt, orc, cuda, leaf):
+def test_collapsed_leaves_same_hits(rt, orc, cuda, leaf, width):
     tris, ubo, rays = rt.gen_config1()
-    with rt.Scene(tris) as base, rt.Scene(tris, leaf_size=leaf) as sc:
+    with rt.Scene(tris, node_width=width) as base, rt.Scene(tris, leaf_size=leaf, node_width=width) as sc:
         a = dev_trace(rt, cuda, base, rays)
         b = dev_trace(rt, cuda, sc, rays)
         assert sc.info().device_nodes < base.info().device_nodes
@@ -55,10 +58,11 @@ def test_collapsed_leaves_same_hits(rt, orc, cuda, leaf):
     assert_parity(orc, tris, rays, a, b)
 
 
-def test_soup_matches_oracle(rt, orc, cuda):
+@pytest.mark.parametrize("width", [2, 4])
+def test_soup_matches_oracle(rt, orc, cuda, width):
     tris = rt.gen_soup(11, 0, 200_000, 1.0, 0.004)
     rays = rt.gen_rays(11, 0, 300_000, 1.0, 1e-4, float("inf"))
-    with rt.Scene(tris) as sc:
+    with rt.Scene(tris, node_width=width) as sc:
         got = dev_trace(rt, cuda, sc, rays)
         S = orc.Scene(tris, sc.nodes())
     can, _ = orc.trace(S, rays, canonical=True)
@@ -67,10 +71,11 @@ def test_soup_matches_oracle(rt, orc, cuda):
     assert_parity(orc, tris, rays[:20000], ref, got[:20000])
 
 
-def test_any_hit_semantics(rt, orc, cuda):
+@pytest.mark.parametrize("width", [2, 4])
+def test_any_hit_semantics(rt, orc, cuda, width):
     tris = rt.gen_soup(12, 0, 100_000, 1.0, 0.004)
     rays = rt.gen_rays(12, 0, 100_000, 1.0, 1e-4, 0.05)
-    with rt.Scene(tris) as sc:
+    with rt.Scene(tris, node_width=width) as sc:
         anyh = dev_trace(rt, cuda, sc, rays, any_hit=True)
         close = dev_trace(rt, cuda, sc, rays)
         ref, _ = orc.trace(orc.Scene(tris, sc.nodes()), rays, canonical=True)
@@ -125,7 +130,8 @@ def test_caller_supplied_nodes(rt, orc, cuda):
     assert np.array_equal(a.view(np.uint64), b.view(np.uint64))
 
 
-def test_spheres_and_models(rt, orc, cuda):
+@pytest.mark.parametrize("width", [2, 4])
+def test_spheres_and_models(rt, orc, cuda, width):
     tris = rt.gen_icosphere(2, (0.0, 0.0, 0.0), 1.0, 0)
     tris["modelIndex"] = 0
     sph = np.zeros(3, rt.SPHERE_DTYPE)
@@ -140,7 +146,7 @@ def test_spheres_and_models(rt, orc, cuda):
     models[1]["m"] = m.T.ravel()  # column-major
     ubo = rt.make_ubo((0.0, 0.5, 6.0), (0.0, 0.0, 0.0), fov=70.0)
     rays = rt.gen_camera_rays(ubo, 160, 90)
-    with rt.Scene(tris, spheres=sph, models=models) as sc:
+    with rt.Scene(tris, spheres=sph, models=models, node_width=width) as sc:
         got = dev_trace(rt, cuda, sc, rays)
         nodes = sc.nodes()
     onodes, _, _, _ = orc.build_bvh(tris, sph, mode=0, models=models["m"])
@@ -178,7 +184,8 @@ def world(rt, tris, sph, models):
     return wt, ws
 
 
-def test_edge_cases(rt, orc, cuda):
+@pytest.mark.parametrize("width", [2, 4])
+def test_edge_cases(rt, orc, cuda, width):
     # one triangle; axis-aligned and grazing rays; ray starting on the triangle; tmax < tmin
     t = np.zeros(2, rt.TRIANGLE_DTYPE)
     t[0]["v0"][:3] = (0, 0, 0)
@@ -200,17 +207,24 @@ def test_edge_cases(rt, orc, cuda):
     r[5]["tmin"], r[5]["tmax"] = 2.0, 1.0                         # empty interval
     r[6]["org"], r[6]["dir"] = (5.5, 5.5, 4.0), (0, 0, 1)         # through the zero-area one
     r[7]["org"], r[7]["dir"] = (1.0, 0.0, 1.0), (0, 0, -1)        # exactly on a vertex
-    with rt.Scene(t) as sc:
+    with rt.Scene(t, node_width=width) as sc:
         got = dev_trace(rt, cuda, sc, r)
         ref, _ = orc.trace(orc.Scene(t, sc.nodes()), r)
-    assert np.array_equal(got["prim"], ref["prim"]), (got, ref)
+    # Ray 7 lies in the plane x = 1 of the leaf box's face with d.x = 0: the
+    # reference's slab test computes 0/0 there and rejects the box, the kernels
+    # keep a box whose face the ray touches.  The vertex hit they may report
+    # must pass the reference's own triangle test.
+    if got["prim"][7] != ref["prim"][7]:
+        assert ref["prim"][7] == orc.NO_HIT and orc.triangle_test(t[got["prim"][7]], r[7:8]) == got["t"][7]
+    keep = np.arange(len(r)) != 7
+    assert np.array_equal(got["prim"][keep], ref["prim"][keep]), (got, ref)
     assert list(got["prim"][:2]) == [0, 0]
     assert got["prim"][2] == orc.NO_HIT and got["prim"][4] == orc.NO_HIT and got["prim"][5] == orc.NO_HIT
     assert got["prim"][6] == orc.NO_HIT
-    hit = ref["prim"] != orc.NO_HIT
+    hit = (ref["prim"] != orc.NO_HIT) & keep
     assert np.array_equal(got["t"][hit], ref["t"][hit])
     # empty scene: every ray misses; zero rays is a no-op
-    with rt.Scene(np.zeros(0, rt.TRIANGLE_DTYPE)) as empty:
+    with rt.Scene(np.zeros(0, rt.TRIANGLE_DTYPE), node_width=width) as empty:
         g = dev_trace(rt, cuda, empty, r)
         assert np.all(g["prim"] == orc.NO_HIT)
         empty.trace(cuda.empty(0, dtype=cuda.uint8, device="cuda"), cuda.empty(0, dtype=cuda.uint8, device="cuda"), n=0)
@@ -235,3 +249,17 @@ def test_golden_fixtures_on_gpu(rt, orc, cuda):
     with rt.Scene(st) as sc:
         got = dev_trace(rt, cuda, sc, sr)
     assert_parity(orc, st, sr, s["hits"].view(rt.HIT_DTYPE), got)
+
+
+@pytest.mark.parametrize("width", [2, 4])
+def test_work_counters(rt, cuda, width):
+    tris = rt.gen_soup(14, 0, 100_000, 1.0, 0.004)
+    rays = rt.gen_rays(14, 0, 200_000, 1.0, 1e-4, float("inf"))
+    with rt.Scene(tris, node_width=width) as sc:
+        d_rays = cuda.from_numpy(rays.view(np.uint8)).cuda()
+        a = cuda.empty(len(rays) * 8, dtype=cuda.uint8, device="cuda")
+        b = cuda.empty_like(a)
+        sc.trace(d_rays, a)
+        nodes, tests = sc.trace_count(d_rays, b)
+    assert cuda.equal(a, b)
+    assert nodes > len(rays) and tests > len(rays) // 2
