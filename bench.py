@@ -49,7 +49,7 @@ COUNT_SAMPLE = 65_536
 def parse():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
-    p.add_argument("--steps", type=int, default=20)
+    p.add_argument("--steps", type=int, default=40)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
     p.add_argument("--tris", type=int, default=N_TRIS)
@@ -59,6 +59,7 @@ def parse():
     p.add_argument("--cpu-sample", type=int, default=CPU_SAMPLE)
     p.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--no-sort", action="store_true", help="trace in the given ray order (no RT_TRACE_SORT)")
     return p.parse_args()
 
 
@@ -229,10 +230,11 @@ def run_ours(args):
         if dist is not None:
             dist.barrier()
 
+    sort = not args.no_sort
     for _ in range(args.warmup):
-        scene.trace(d_rays, d_hits)
+        scene.trace(d_rays, d_hits, sort=sort)
     torch.cuda.synchronize()
-    gpu_nodes, gpu_tests = scene.trace_count(d_rays, d_hits)
+    gpu_nodes, gpu_tests = scene.trace_count(d_rays, d_hits, sort=sort)
     clocks = ClockSampler(local)
     clocks.start()
     time.sleep(0.5)
@@ -245,7 +247,7 @@ def run_ours(args):
     g0.record(stream)
     for s in range(args.steps):
         evs[s][0].record(stream)
-        scene.trace(d_rays, d_hits, stream=stream)
+        scene.trace(d_rays, d_hits, sort=sort, stream=stream)
         evs[s][1].record(stream)
     g1.record(stream)
     torch.cuda.synchronize()
@@ -266,12 +268,12 @@ def run_ours(args):
         h_hits = torch.empty(n * 8, dtype=torch.uint8).pin_memory()
         hr = h_rays.numpy().view(rt.RAY_DTYPE)
         hh = h_hits.numpy().view(rt.HIT_DTYPE)
-        scene.trace_host(hr, out=hh)
+        scene.trace_host(hr, out=hh, sort=sort)
         k = max(3, min(args.steps, 10))
         barrier()
         t0 = time.perf_counter()
         for _ in range(k):
-            scene.trace_host(hr, out=hh)
+            scene.trace_host(hr, out=hh, sort=sort)
         dt = time.perf_counter() - t0
         barrier()
         e2e = {"value": n * ws / (dt / k) / 1e9, "unit": UNIT, "h2d_bytes_per_step": n * 32,
@@ -302,7 +304,8 @@ def run_ours(args):
                 "traffic": None, "peak_kind": peak_kind,
                 "bytes_per_ray": b_ray, "node_boxes_per_ray": counts["node_boxes_per_ray"],
                 "tri_tests_per_ray": counts["tri_tests_per_ray"],
-                "kernel": f"k_trace<closest> (persistent warps, {info.node_width}-wide nodes)",
+                "kernel": f"k_trace_step<closest> (persistent warps, {info.node_width}-wide nodes)"
+                          + ("; the step also runs the 3 reorder kernels" if sort else ""),
                 "gpu_node_fetches_per_ray": gpu_nodes / n, "gpu_prim_tests_per_ray": gpu_tests / n,
                 "fetched_bytes_per_ray": 40 + 64 * gpu_nodes / n + 64 * gpu_tests / n,
                 "avg_launch_ms": avg_launch * 1e3}
@@ -316,9 +319,10 @@ def run_ours(args):
                        "leaf_size": info.leaf_size, "node_width": info.node_width,
                        "device_nodes": info.device_nodes, "bvh_depth": info.depth, "stack_need": info.stack_need,
                        "l2": "inputs larger than L2 (rays 512 MiB, nodes+triangles 512 MiB); no flush",
+                       "ray_order": "origin-bucketed inside the step (RT_TRACE_SORT)" if sort else "as given",
                        "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU"},
             "roofline": roof, "cpu_baseline": cpu_base, "e2e": e2e, "clocks": clk,
-            "gpu_launches": args.steps, "parity_sample": parity,
+            "gpu_launches": args.steps * (4 if sort else 1), "parity_sample": parity,
             "scene_build_s": info.build_seconds}
     print(json.dumps(line), flush=True)
     if dist is not None:

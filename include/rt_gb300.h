@@ -209,7 +209,10 @@ rt_status rt_build_bvh(const RtTriangle64* triangles, uint32_t num_triangles,
 /* ------------------------------------------------------------------ trace */
 enum {
   RT_TRACE_CLOSEST = 0,  /* closest hit in [tmin, tmax] (hitBVH, raytraceBVH.comp:195-265) */
-  RT_TRACE_ANY = 1       /* any hit in [tmin, tmax] (occlusion) */
+  RT_TRACE_ANY = 1,      /* any hit in [tmin, tmax] (occlusion) */
+  RT_TRACE_SORT = 2      /* or'ed in: trace the batch in an order bucketed by ray origin
+                            (coherence); hits are unchanged and still land in ray order.
+                            Uses a per-stream device workspace of about 6 bytes per ray. */
 };
 
 /* Traces n rays resident on the device; writes n hits.  Stream-ordered. */

@@ -42,6 +42,9 @@ struct Workspace {
   // staging for rt_trace_host
   void* stage = nullptr;
   size_t stage_bytes = 0;
+  // scratch of the coherence reordering
+  void* sort = nullptr;
+  size_t sort_bytes = 0;
   cudaStream_t copy_in = nullptr, copy_out = nullptr;
   cudaEvent_t ev[8] = {};
 };
@@ -68,6 +71,27 @@ static rt_status workspace(cudaStream_t st, Workspace** out) {
   g_ws[key] = w;
   *out = w;
   return RT_OK;
+}
+
+// Reorders the batch when RT_TRACE_SORT is set; *order = nullptr otherwise.
+static rt_status maybe_reorder(Workspace* w, const DeviceScene& d, const RtRay* rays, uint32_t n, uint32_t flags,
+                               cudaStream_t st, uint32_t** order) {
+  *order = nullptr;
+  if (!(flags & RT_TRACE_SORT) || d.root == kSentinel) return RT_OK;
+  const size_t need = reorder_scratch_bytes(n);
+  if (w->sort_bytes < need) {
+    if (w->sort) cudaFree(w->sort);
+    w->sort = nullptr;
+    w->sort_bytes = 0;
+    cudaError_t e = cudaMalloc(&w->sort, need);
+    if (e != cudaSuccess) {
+      set_error(std::string("reorder scratch: cudaMalloc: ") + cudaGetErrorString(e));
+      return RT_ENOMEM;
+    }
+    w->sort_bytes = need;
+  }
+  cudaError_t e = launch_reorder(d, rays, n, w->sort, order, st);
+  return e == cudaSuccess ? RT_OK : cuda_fail(e, "reorder");
 }
 
 }  // namespace rtgb
@@ -223,6 +247,11 @@ rt_status rt_scene_create_ex(const RtSceneDesc* desc, rt_scene** out_scene) {
   sc->d.depth = hb.depth;
   sc->d.width = hb.width;
   sc->d.stack_need = hb.stack_need;
+  if (!sc->nodes40.empty()) {
+    const RtBVHNode40& r = sc->nodes40[0];
+    const float b[6] = {r.minX, r.minY, r.minZ, r.maxX, r.maxY, r.maxZ};
+    for (int k = 0; k < 6; ++k) sc->d.box[k] = b[k];
+  }
   RtSceneInfo& inf = sc->info;
   inf.num_triangles = nt;
   inf.num_spheres = ns;
@@ -289,7 +318,7 @@ rt_status rt_scene_get_nodes(const rt_scene* scene, RtBVHNode40* h_out, uint32_t
 }
 
 rt_status rt_trace(rt_scene* scene, const RtRay* d_rays, uint32_t n, RtHit* d_hits, uint32_t flags, void* stream) {
-  if (!scene || (n && (!d_rays || !d_hits)) || flags > RT_TRACE_ANY || n > 0x80000000u) {
+  if (!scene || (n && (!d_rays || !d_hits)) || flags > (RT_TRACE_ANY | RT_TRACE_SORT) || n > 0x80000000u) {
     set_error("rt_trace: bad argument");
     return RT_EINVAL;
   }
@@ -298,16 +327,19 @@ rt_status rt_trace(rt_scene* scene, const RtRay* d_rays, uint32_t n, RtHit* d_hi
   Workspace* w = nullptr;
   rt_status s = workspace(st, &w);
   if (s != RT_OK) return s;
+  uint32_t* order = nullptr;
+  if ((s = maybe_reorder(w, scene->d, d_rays, n, flags, st, &order)) != RT_OK) return s;
   cudaError_t e = cudaMemsetAsync(w->counters, 0, 2 * sizeof(uint32_t), st);
   if (e != cudaSuccess) return cuda_fail(e, "rt_trace: memset");
-  e = launch_trace(scene->d, d_rays, n, d_hits, flags, w->counters, stream);
+  e = launch_trace(scene->d, d_rays, n, d_hits, flags, w->counters, stream, order);
   if (e != cudaSuccess) return cuda_fail(e, "rt_trace: launch");
   return RT_OK;
 }
 
 rt_status rt_trace_count(rt_scene* scene, const RtRay* d_rays, uint32_t n, RtHit* d_hits, uint32_t flags,
                          void* stream, uint64_t* h_counts) {
-  if (!scene || !h_counts || (n && (!d_rays || !d_hits)) || flags > RT_TRACE_ANY || n > 0x80000000u) {
+  if (!scene || !h_counts || (n && (!d_rays || !d_hits)) || flags > (RT_TRACE_ANY | RT_TRACE_SORT) ||
+      n > 0x80000000u) {
     set_error("rt_trace_count: bad argument");
     return RT_EINVAL;
   }
@@ -320,7 +352,9 @@ rt_status rt_trace_count(rt_scene* scene, const RtRay* d_rays, uint32_t n, RtHit
   cudaError_t e = cudaMemsetAsync(w->counters, 0, 64 * sizeof(uint32_t), st);
   if (e != cudaSuccess) return cuda_fail(e, "rt_trace_count: memset");
   unsigned long long* stats = reinterpret_cast<unsigned long long*>(w->counters + 8);
-  e = launch_trace_tuned(scene->d, d_rays, n, d_hits, flags, w->counters, stream, default_tuning(), stats);
+  uint32_t* order = nullptr;
+  if ((s = maybe_reorder(w, scene->d, d_rays, n, flags, st, &order)) != RT_OK) return s;
+  e = launch_trace_tuned(scene->d, d_rays, n, d_hits, flags, w->counters, stream, default_tuning(), stats, order);
   if (e != cudaSuccess) return cuda_fail(e, "rt_trace_count: launch");
   unsigned long long hc[2] = {0, 0};
   e = cudaMemcpyAsync(hc, stats, sizeof(hc), cudaMemcpyDeviceToHost, st);
@@ -333,7 +367,7 @@ rt_status rt_trace_count(rt_scene* scene, const RtRay* d_rays, uint32_t n, RtHit
 
 rt_status rt_trace_host(rt_scene* scene, const RtRay* h_rays, uint32_t n, RtHit* h_hits, uint32_t flags,
                         void* stream) {
-  if (!scene || (n && (!h_rays || !h_hits)) || flags > RT_TRACE_ANY || n > 0x80000000u) {
+  if (!scene || (n && (!h_rays || !h_hits)) || flags > (RT_TRACE_ANY | RT_TRACE_SORT) || n > 0x80000000u) {
     set_error("rt_trace_host: bad argument");
     return RT_EINVAL;
   }
@@ -386,8 +420,10 @@ rt_status rt_trace_host(rt_scene* scene, const RtRay* h_rays, uint32_t n, RtHit*
       return cuda_fail(e, "rt_trace_host: H2D");
     if ((e = cudaEventRecord(in_done[b], w->copy_in)) != cudaSuccess) return cuda_fail(e, "event");
     if ((e = cudaStreamWaitEvent(st, in_done[b], 0)) != cudaSuccess) return cuda_fail(e, "wait");
+    uint32_t* order = nullptr;
+    if ((s = maybe_reorder(w, scene->d, drays[b], cnt, flags, st, &order)) != RT_OK) return s;
     if ((e = cudaMemsetAsync(w->counters, 0, 2 * sizeof(uint32_t), st)) != cudaSuccess) return cuda_fail(e, "memset");
-    if ((e = launch_trace(scene->d, drays[b], cnt, dhits[b], flags, w->counters, stream)) != cudaSuccess)
+    if ((e = launch_trace(scene->d, drays[b], cnt, dhits[b], flags, w->counters, stream, order)) != cudaSuccess)
       return cuda_fail(e, "rt_trace_host: launch");
     if ((e = cudaEventRecord(trace_done[b], st)) != cudaSuccess) return cuda_fail(e, "event");
     if ((e = cudaStreamWaitEvent(w->copy_out, trace_done[b], 0)) != cudaSuccess) return cuda_fail(e, "wait");

@@ -66,6 +66,7 @@ struct DeviceScene {
   uint32_t depth = 0;
   uint32_t width = 2;       // 2: binary child-box nodes; 4: quantised 4-wide nodes
   uint32_t stack_need = 0;  // worst-case traversal stack entries
+  float box[6] = {0, 0, 0, 0, 0, 0};  // root box: lo xyz, hi xyz
 };
 
 // Host-side result of the BVH conversion, ready to upload.
@@ -139,10 +140,15 @@ int num_trace_variants();
 void trace_variant_shape(int v, int* threads, int* minb);
 cudaError_t launch_trace_tuned(const DeviceScene& s, const RtRay* rays, uint32_t n, RtHit* hits, uint32_t flags,
                                uint32_t* counter, void* stream, const TraceTuning& tune,
-                               unsigned long long* stats);
+                               unsigned long long* stats, const uint32_t* order);
+// Coherence reordering (reorder.cu): bytes of scratch for n rays, and the
+// launch that leaves the ray order (a permutation of 0..n-1) in *order_out.
+size_t reorder_scratch_bytes(uint32_t n);
+cudaError_t launch_reorder(const DeviceScene& s, const RtRay* rays, uint32_t n, void* scratch, uint32_t** order_out,
+                           void* stream);
 // Kernels launch on the given stream; counter is a device uint32 zeroed by the caller.
 cudaError_t launch_trace(const DeviceScene& s, const RtRay* rays, uint32_t n, RtHit* hits, uint32_t flags,
-                         uint32_t* counter, void* stream);
+                         uint32_t* counter, void* stream, const uint32_t* order = nullptr);
 cudaError_t launch_render(const DeviceScene& s, const float cam[12], uint32_t depth, uint32_t random_state,
                           float* accum, uint32_t w, uint32_t h, uint32_t spp, uint32_t shade_mode,
                           const float bg[3], uint32_t* counter, void* stream);

@@ -32,7 +32,8 @@ __device__ __forceinline__ uint32_t lanemask_lt() {
 template <bool ANY, int STACK, int THREADS, int MINB, int W, bool STATS>
 __global__ void __launch_bounds__(THREADS, MINB)
     k_trace(DeviceScene S, const float4* __restrict__ rays, uint32_t n, uint2* __restrict__ hits,
-            uint32_t* __restrict__ counter, int refill, unsigned long long* __restrict__ stats) {
+            uint32_t* __restrict__ counter, int refill, unsigned long long* __restrict__ stats,
+            const uint32_t* __restrict__ order) {
   using StackT = typename std::conditional<W == 2, uint32_t, uint2>::type;
   StackT stack[STACK];
   dev::Trav s;
@@ -51,8 +52,8 @@ __global__ void __launch_bounds__(THREADS, MINB)
       if (idle) {
         const uint32_t id = base + (uint32_t)__popc(m & lanemask_lt());
         if (id < n) {
-          ray = id;
-          dev::trav_init_ray(s, __ldg(&rays[2u * id]), __ldg(&rays[2u * id + 1u]), S.root);
+          ray = order ? __ldg(&order[id]) : id;
+          dev::trav_init_ray(s, __ldg(&rays[2u * ray]), __ldg(&rays[2u * ray + 1u]), S.root);
           if constexpr (W == 2) stack[0] = kSentinel;
         }
       }
@@ -104,7 +105,8 @@ __global__ void __launch_bounds__(THREADS, MINB)
 template <bool ANY, int STACK, int THREADS, int MINB, bool STATS>
 __global__ void __launch_bounds__(THREADS, MINB)
     k_trace_step(DeviceScene S, const float4* __restrict__ rays, uint32_t n, uint2* __restrict__ hits,
-                 uint32_t* __restrict__ counter, int refill, unsigned long long* __restrict__ stats) {
+                 uint32_t* __restrict__ counter, int refill, unsigned long long* __restrict__ stats,
+            const uint32_t* __restrict__ order) {
   uint2 stack[STACK];
   dev::Trav s;
   const uint32_t lane = threadIdx.x & 31u;
@@ -123,8 +125,8 @@ __global__ void __launch_bounds__(THREADS, MINB)
       if (ray == 0xFFFFFFFFu) {
         const uint32_t id = base + (uint32_t)__popc(idle & lanemask_lt());
         if (id < n) {
-          ray = id;
-          dev::trav_init_ray(s, __ldg(&rays[2u * id]), __ldg(&rays[2u * id + 1u]), S.root);
+          ray = order ? __ldg(&order[id]) : id;
+          dev::trav_init_ray(s, __ldg(&rays[2u * ray]), __ldg(&rays[2u * ray + 1u]), S.root);
           if (s.leaf != 0u) {  // the whole tree is one leaf
             s.node = s.leaf;
             s.leaf = 0u;
@@ -174,7 +176,8 @@ __global__ void __launch_bounds__(THREADS, MINB)
   }
 }
 
-using TraceKernel = void (*)(DeviceScene, const float4*, uint32_t, uint2*, uint32_t*, int, unsigned long long*);
+using TraceKernel = void (*)(DeviceScene, const float4*, uint32_t, uint2*, uint32_t*, int, unsigned long long*,
+                             const uint32_t*);
 
 // Stack capacities: binary trees 64 or 128 refs (depth + sentinel); 4-wide
 // trees 64 or 192 (ref, t) entries (worst-case pushes along a path).
@@ -253,10 +256,11 @@ void trace_variant_shape(int v, int* threads, int* minb) {
 }
 
 cudaError_t launch_trace_tuned(const DeviceScene& S, const RtRay* rays, uint32_t n, RtHit* hits, uint32_t flags,
-                               uint32_t* counter, void* stream, const TraceTuning& tune, unsigned long long* stats) {
+                               uint32_t* counter, void* stream, const TraceTuning& tune, unsigned long long* stats,
+                               const uint32_t* order) {
   const int vi = (tune.variant >= 0 && tune.variant < kNumVariants) ? tune.variant : 0;
   Variant& v = g_variants[vi];
-  const int any = (flags & RT_TRACE_ANY) != 0 ? 1 : 0;
+  const int any = (flags & RT_TRACE_ANY) != 0 ? 1 : 0;  // RT_TRACE_SORT is handled by the caller
   const int wide = S.width == 4 ? 1 : 0;
   const int big = S.stack_need > 64u ? 1 : 0;
   const int st = stats ? 1 : 0;
@@ -275,7 +279,7 @@ cudaError_t launch_trace_tuned(const DeviceScene& S, const RtRay* rays, uint32_t
   if (blocks > needed) blocks = needed;
   if (blocks == 0) blocks = 1;
   k<<<(uint32_t)blocks, v.threads, 0, reinterpret_cast<cudaStream_t>(stream)>>>(
-      S, reinterpret_cast<const float4*>(rays), n, reinterpret_cast<uint2*>(hits), counter, tune.refill, stats);
+      S, reinterpret_cast<const float4*>(rays), n, reinterpret_cast<uint2*>(hits), counter, tune.refill, stats, order);
   return cudaGetLastError();
 }
 
@@ -290,8 +294,8 @@ int device_sm_count() {
 }
 
 cudaError_t launch_trace(const DeviceScene& s, const RtRay* rays, uint32_t n, RtHit* hits, uint32_t flags,
-                         uint32_t* counter, void* stream) {
-  return launch_trace_tuned(s, rays, n, hits, flags, counter, stream, default_tuning(), nullptr);
+                         uint32_t* counter, void* stream, const uint32_t* order) {
+  return launch_trace_tuned(s, rays, n, hits, flags, counter, stream, default_tuning(), nullptr, order);
 }
 
 // ---- allocation-free ray queries (rt_trace_noalloc) ----

@@ -11,11 +11,11 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 
-def dev_trace(rt, torch, scene, rays, any_hit=False):
+def dev_trace(rt, torch, scene, rays, any_hit=False, sort=False):
     rays = np.ascontiguousarray(rays, dtype=rt.RAY_DTYPE)
     d_rays = torch.from_numpy(rays.view(np.uint8)).cuda()
     d_hits = torch.full((max(len(rays), 1) * 8,), 0xAB, dtype=torch.uint8, device="cuda")
-    scene.trace(d_rays, d_hits, n=len(rays), any_hit=any_hit)
+    scene.trace(d_rays, d_hits, n=len(rays), any_hit=any_hit, sort=sort)
     torch.cuda.synchronize()
     return d_hits.cpu().numpy().view(rt.HIT_DTYPE)[: len(rays)]
 
@@ -96,10 +96,10 @@ def test_config3_full_size(rt, orc, cuda):
     rays = rt.gen_rays(3, 0, 16_777_216, 1.0, 1e-4, float("inf"))
     with rt.Scene(tris) as sc:
         got = dev_trace(rt, cuda, sc, rays)
-        again = dev_trace(rt, cuda, sc, rays)
-        anyh = dev_trace(rt, cuda, sc, rays, any_hit=True)
+        again = dev_trace(rt, cuda, sc, rays, sort=True)
+        anyh = dev_trace(rt, cuda, sc, rays, any_hit=True, sort=True)
         S = orc.Scene(tris, sc.nodes())
-    assert np.array_equal(got.view(np.uint64), again.view(np.uint64))
+    assert np.array_equal(got.view(np.uint64), again.view(np.uint64))  # reordering changes nothing
     assert np.array_equal(got["prim"] != orc.NO_HIT, anyh["prim"] != orc.NO_HIT)
     can, _ = orc.trace(S, rays, canonical=True)
     arb = assert_parity(orc, tris, rays, can, got)
@@ -263,3 +263,21 @@ def test_work_counters(rt, cuda, width):
         nodes, tests = sc.trace_count(d_rays, b)
     assert cuda.equal(a, b)
     assert nodes > len(rays) and tests > len(rays) // 2
+
+
+@pytest.mark.parametrize("width", [2, 4])
+def test_sorted_order_same_hits(rt, cuda, width):
+    tris = rt.gen_soup(15, 0, 150_000, 1.0, 0.004)
+    rays = rt.gen_rays(15, 0, 1_000_003, 1.0, 1e-4, float("inf"))
+    cam_tris, ubo, cam_rays = rt.gen_config1()
+    with rt.Scene(tris, node_width=width) as sc, rt.Scene(cam_tris, node_width=width) as cam:
+        for anyh in (False, True):
+            a = dev_trace(rt, cuda, sc, rays, any_hit=anyh)
+            b = dev_trace(rt, cuda, sc, rays, any_hit=anyh, sort=True)
+            assert np.array_equal(a.view(np.uint64), b.view(np.uint64))
+        # every camera ray starts at one point: a single bucket
+        a = dev_trace(rt, cuda, cam, cam_rays)
+        b = dev_trace(rt, cuda, cam, cam_rays, sort=True)
+        assert np.array_equal(a.view(np.uint64), b.view(np.uint64))
+        c = sc.trace_host(rays[:300_000], sort=True)
+        assert np.array_equal(c.view(np.uint64), dev_trace(rt, cuda, sc, rays[:300_000]).view(np.uint64))
