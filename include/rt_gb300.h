@@ -256,6 +256,60 @@ rt_status rt_trace_count(rt_scene* scene, const RtRay* d_rays, uint32_t n, RtHit
 rt_status rt_trace_noalloc(rt_scene* scene, const RtRay* d_rays, uint32_t n, RtHit* d_hits,
                            uint32_t flags, void* stream);
 
+/* ------------------------------------------------------------ scene pool */
+/* Resident scenes sharing one device arena, traced together in one launch.
+ * No counterpart in the reference, which traces one scene per frame; this is
+ * the batched form of rt_trace: many scenes of uneven size, each with its own
+ * ray batch, traced by one persistent launch replayed from a captured CUDA
+ * graph, with the launch shape picked by rt_pool_autotune.  Pooled scenes hold
+ * triangles only and use the 4-wide device BVH; at most 2^27 triangles per pool. */
+typedef struct rt_pool rt_pool;
+
+typedef struct RtPoolOptions {
+  uint64_t budget_bytes;  /* device bytes the scenes may occupy (nodes + triangles); 0 = 8 GiB */
+  uint32_t max_scenes;    /* 0 = 4096 */
+  uint32_t _reserved;
+} RtPoolOptions;
+
+typedef struct RtPoolInfo {
+  uint32_t num_scenes;
+  uint32_t stack_need;    /* worst-case traversal stack over the pooled scenes */
+  uint64_t used_bytes;    /* scene bytes accounted against the budget */
+  uint64_t budget_bytes;
+  uint64_t arena_bytes;   /* device memory the arena holds */
+  uint32_t num_triangles;
+  uint32_t tuned_variant; /* launch shape in use (see rt_pool_describe_variant) */
+  int32_t tuned_refill;   /* idle lanes that trigger a ray refill */
+  uint32_t _pad;
+} RtPoolInfo;
+
+typedef struct RtJob {    /* one scene's ray batch */
+  uint32_t scene_id;
+  uint32_t num_rays;
+  const RtRay* d_rays;    /* device */
+  RtHit* d_hits;          /* device */
+} RtJob;
+
+rt_status rt_pool_create(const RtPoolOptions* opt, rt_pool** out_pool);
+rt_status rt_pool_destroy(rt_pool* pool);
+/* Builds the scene's BVH on the host like rt_scene_create_ex and uploads it
+ * into the arena.  RT_ENOMEM when it would exceed the budget, RT_EBUSY at the
+ * scene limit, RT_EUNSUPPORTED for spheres. */
+rt_status rt_pool_add_scene(rt_pool* pool, const RtSceneDesc* desc, uint32_t* out_scene_id);
+/* Frees the scene's arena ranges; no batch using it may still be in flight. */
+rt_status rt_pool_remove_scene(rt_pool* pool, uint32_t scene_id);
+rt_status rt_pool_get_info(const rt_pool* pool, RtPoolInfo* out_info);
+/* Traces all jobs (at most 8192, 2^31 rays) in one persistent launch, stream-
+ * ordered.  flags: RT_TRACE_CLOSEST or RT_TRACE_ANY for every job.  Hits are
+ * identical to rt_trace on each scene alone. */
+rt_status rt_pool_trace(rt_pool* pool, const RtJob* jobs, uint32_t num_jobs, uint32_t flags, void* stream);
+/* Times the jobs under every launch shape (threads per block, register cap)
+ * and refill threshold, `repeats` launches each, and keeps the fastest for
+ * later rt_pool_trace calls.  Synchronous. */
+rt_status rt_pool_autotune(rt_pool* pool, const RtJob* jobs, uint32_t num_jobs, uint32_t flags, void* stream,
+                           uint32_t repeats);
+rt_status rt_pool_describe_variant(uint32_t variant, uint32_t* threads, uint32_t* min_blocks);
+
 /* ----------------------------------------------------------------- render */
 enum {
   RT_SHADE_REFERENCE = 0, /* LIGHT emits, DIFFUSE scatters, others terminate, background 0 */

@@ -82,6 +82,21 @@ class SceneInfo(C.Structure):
                 ("build_seconds", C.c_double), ("node_width", C.c_uint32), ("stack_need", C.c_uint32)]
 
 
+class PoolOptions(C.Structure):
+    _fields_ = [("budget_bytes", C.c_uint64), ("max_scenes", C.c_uint32), ("_reserved", C.c_uint32)]
+
+
+class PoolInfo(C.Structure):
+    _fields_ = [("num_scenes", C.c_uint32), ("stack_need", C.c_uint32), ("used_bytes", C.c_uint64),
+                ("budget_bytes", C.c_uint64), ("arena_bytes", C.c_uint64), ("num_triangles", C.c_uint32),
+                ("tuned_variant", C.c_uint32), ("tuned_refill", C.c_int32), ("_pad", C.c_uint32)]
+
+
+class Job(C.Structure):
+    """RtJob: one scene's ray batch (device buffers)."""
+    _fields_ = [("scene_id", C.c_uint32), ("num_rays", C.c_uint32), ("d_rays", C.c_void_p), ("d_hits", C.c_void_p)]
+
+
 class _RenderOptions(C.Structure):
     _fields_ = [("shade_mode", C.c_uint32), ("background", C.c_float * 3)]
 
@@ -109,6 +124,14 @@ SIGNATURES = {
     "rt_last_error_string": (C.c_char_p, []),
     "rt_abi_version": (_U32, []),
     "rt_stream_wait": (_I, [_P, _D]),
+    "rt_pool_create": (_I, [C.POINTER(PoolOptions), C.POINTER(C.c_void_p)]),
+    "rt_pool_destroy": (_I, [_P]),
+    "rt_pool_add_scene": (_I, [_P, C.POINTER(_SceneDesc), C.POINTER(_U32)]),
+    "rt_pool_remove_scene": (_I, [_P, _U32]),
+    "rt_pool_get_info": (_I, [_P, C.POINTER(PoolInfo)]),
+    "rt_pool_trace": (_I, [_P, C.POINTER(Job), _U32, _U32, _P]),
+    "rt_pool_autotune": (_I, [_P, C.POINTER(Job), _U32, _U32, _P, _U32]),
+    "rt_pool_describe_variant": (_I, [_U32, C.POINTER(_U32), C.POINTER(_U32)]),
     "rt_gen_uniform": (_I, [_U64, _U64, _U64, _P]),
     "rt_gen_icosphere": (_I, [_U32, _P, _F, _U32, _P, _U64, C.POINTER(_U64)]),
     "rt_gen_config1": (_I, [_P, C.POINTER(RaytracingUBO), _P]),
@@ -267,6 +290,93 @@ class Scene:
 
     def __exit__(self, *a):
         self.close()
+
+
+def _desc(triangles, models=None, nodes=None, bvh_mode=BVH_SORTED, leaf_size=0, node_width=0):
+    tri = np.ascontiguousarray(triangles, dtype=TRIANGLE_DTYPE)
+    mod = np.ascontiguousarray(models, dtype=MODEL_DTYPE) if models is not None else None
+    nod = np.ascontiguousarray(nodes, dtype=NODE_DTYPE) if nodes is not None else None
+    d = _SceneDesc(_ptr(tri), len(tri), None, 0, None, 0, _ptr(mod), 0 if mod is None else len(mod),
+                   _ptr(nod), 0 if nod is None else len(nod), bvh_mode, leaf_size, node_width)
+    return d, (tri, mod, nod)
+
+
+class Pool:
+    """Resident scenes in one device arena, traced together (rt_pool_*).
+
+    add_scene() admits a scene against the byte budget; trace() runs every
+    job -- (scene_id, device rays, device hits[, n]) -- in one persistent,
+    graph-replayed launch; autotune() picks the launch shape for a batch."""
+
+    def __init__(self, budget_bytes: int = 0, max_scenes: int = 0):
+        opt = PoolOptions(budget_bytes, max_scenes, 0)
+        h = C.c_void_p()
+        _check(lib().rt_pool_create(C.byref(opt), C.byref(h)), "rt_pool_create")
+        self._h = h
+
+    @property
+    def handle(self) -> int:
+        if self._h is None:
+            raise ValueError("pool destroyed")
+        return self._h.value
+
+    def add_scene(self, triangles, models=None, nodes=None, bvh_mode: int = BVH_SORTED, leaf_size: int = 0) -> int:
+        d, keep = _desc(triangles, models, nodes, bvh_mode, leaf_size, 4)
+        sid = C.c_uint32()
+        _check(lib().rt_pool_add_scene(self.handle, C.byref(d), C.byref(sid)), "rt_pool_add_scene")
+        return sid.value
+
+    def remove_scene(self, scene_id: int) -> None:
+        _check(lib().rt_pool_remove_scene(self.handle, scene_id), "rt_pool_remove_scene")
+
+    def info(self) -> PoolInfo:
+        inf = PoolInfo()
+        _check(lib().rt_pool_get_info(self.handle, C.byref(inf)), "rt_pool_get_info")
+        return inf
+
+    @staticmethod
+    def _jobs(jobs):
+        arr = (Job * max(len(jobs), 1))()
+        for i, j in enumerate(jobs):
+            sid, rays, hits = j[0], j[1], j[2]
+            n = j[3] if len(j) > 3 else rays.numel() * rays.element_size() // RAY_DTYPE.itemsize
+            arr[i] = Job(sid, n, _ptr(rays), _ptr(hits))
+        return arr
+
+    def trace(self, jobs, any_hit: bool = False, stream=None) -> None:
+        arr = self._jobs(jobs)
+        _check(lib().rt_pool_trace(self.handle, arr, len(jobs), TRACE_ANY if any_hit else TRACE_CLOSEST,
+                                   _stream_handle(stream)), "rt_pool_trace")
+
+    def autotune(self, jobs, any_hit: bool = False, repeats: int = 3, stream=None) -> tuple[int, int]:
+        arr = self._jobs(jobs)
+        _check(lib().rt_pool_autotune(self.handle, arr, len(jobs), TRACE_ANY if any_hit else TRACE_CLOSEST,
+                                      _stream_handle(stream), repeats), "rt_pool_autotune")
+        inf = self.info()
+        return inf.tuned_variant, inf.tuned_refill
+
+    def close(self) -> None:
+        if getattr(self, "_h", None) is not None and self._h.value:
+            lib().rt_pool_destroy(self._h.value)
+        self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+
+def describe_pool_variant(v: int) -> tuple[int, int]:
+    t, m = C.c_uint32(), C.c_uint32()
+    _check(lib().rt_pool_describe_variant(v, C.byref(t), C.byref(m)), "rt_pool_describe_variant")
+    return t.value, m.value
 
 
 def build_bvh(triangles, spheres=None, models=None, bvh_mode: int = BVH_SORTED) -> np.ndarray:

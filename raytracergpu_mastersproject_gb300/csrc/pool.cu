@@ -1,0 +1,686 @@
+// pool.cu -- resident scenes in one device arena, traced together.
+//
+// The batched form of rt_trace: many scenes of uneven size, each with its own
+// ray batch, traced by one persistent launch that takes rays from a single
+// queue spanning every job.  All scenes of a pool live in one arena -- one
+// array of 4-wide inner nodes, one of triangle records, one of triangle ids --
+// and their child refs are rebased at upload, so a ray only needs its scene's
+// root ref; nothing else in the traversal depends on the scene.
+//
+// Arena ranges are handed out first-fit from free lists and the arrays grow by
+// doubling; refs are indices, so growing (copy to a larger array) keeps them
+// valid.  Scene bytes are accounted against a budget (admission control).
+// Per stream, two launch slots alternate: each holds a pinned job table, its
+// device copy and a captured CUDA graph (table upload, queue reset, kernel).
+#include <cuda_runtime.h>
+
+#include <chrono>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <unordered_map>
+
+#include "trace_core.cuh"
+
+namespace rtgb {
+
+void set_error(const std::string& msg);
+
+namespace {
+
+struct DJob {
+  const float4* rays;
+  uint2* hits;
+  uint32_t start;
+  uint32_t count;
+  uint32_t root;
+  uint32_t pad;
+};
+static_assert(sizeof(DJob) == 32, "job record is 32 bytes");
+
+// Table: header (num_jobs, total, 6 pad words) then the jobs.
+constexpr uint32_t kMaxJobs = 8192;
+constexpr size_t kTableBytes = sizeof(DJob) * (kMaxJobs + 1);
+
+__device__ __forceinline__ uint32_t lanemask_lt_p() {
+  uint32_t m;
+  asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+  return m;
+}
+
+__device__ __forceinline__ uint32_t find_job(const DJob* __restrict__ jobs, uint32_t num, uint32_t g) {
+  uint32_t lo = 0, hi = num;
+  while (hi - lo > 1) {
+    const uint32_t mid = (lo + hi) >> 1;
+    if (__ldg(&jobs[mid].start) <= g) lo = mid;
+    else hi = mid;
+  }
+  return lo;
+}
+
+// k_trace_step over a job table (see trace.cu): each lane keeps (job, local
+// ray index) and its job's root; hits go to the job's own hit array.
+template <bool ANY, int STACK, int THREADS, int MINB>
+__global__ void __launch_bounds__(THREADS, MINB)
+    k_pool_step(DeviceScene S, const DJob* __restrict__ table, uint32_t* __restrict__ counter, int refill) {
+  uint2 stack[STACK];
+  dev::Trav s;
+  const uint32_t lane = threadIdx.x & 31u;
+  const uint32_t num_jobs = __ldg(reinterpret_cast<const uint32_t*>(table));
+  const uint32_t total = __ldg(reinterpret_cast<const uint32_t*>(table) + 1);
+  const DJob* jobs = table + 1;
+  uint32_t job = 0, local = 0xFFFFFFFFu;
+  bool exhausted = total == 0;
+  const int min_idle = refill < 1 ? 1 : (refill > 32 ? 32 : refill);
+  for (;;) {
+    const uint32_t idle = __ballot_sync(0xFFFFFFFFu, local == 0xFFFFFFFFu);
+    if (exhausted && idle == 0xFFFFFFFFu) break;
+    if (!exhausted && __popc(idle) >= min_idle) {
+      uint32_t base = 0;
+      if (lane == 0) base = atomicAdd(counter, (uint32_t)__popc(idle));
+      base = __shfl_sync(0xFFFFFFFFu, base, 0);
+      if (base + (uint32_t)__popc(idle) >= total) exhausted = true;
+      if (local == 0xFFFFFFFFu) {
+        const uint32_t g = base + (uint32_t)__popc(idle & lanemask_lt_p());
+        if (g < total) {
+          job = find_job(jobs, num_jobs, g);
+          local = g - __ldg(&jobs[job].start);
+          const float4* rays = jobs[job].rays;
+          dev::trav_init_ray(s, __ldg(&rays[2u * local]), __ldg(&rays[2u * local + 1u]), __ldg(&jobs[job].root));
+          if (s.leaf != 0u) {
+            s.node = s.leaf;
+            s.leaf = 0u;
+          }
+        }
+      }
+    }
+    if (local == 0xFFFFFFFFu) continue;
+    bool done = false;
+    if (dev::is_inner(s.node)) {
+      if (!dev::visit_wide<STACK>(S, s, stack)) done = true;
+    } else if (dev::is_leaf(s.node)) {
+      if (dev::leaf_visit<ANY>(S, s, s.node))
+        done = true;
+      else
+        s.node = dev::pop_wide(s, stack);
+    }
+    if (done || s.node == kSentinel) {
+      uint2 h;
+      if (s.sp < 0 || s.best == dev::kNoBest) {
+        h.x = RT_NO_HIT;
+        h.y = __float_as_uint(__int_as_float(0x7f800000));
+      } else {
+        h.x = __ldg(&S.tri_ids[s.best & kSlotMask]);
+        h.y = __float_as_uint(s.tclose);
+      }
+      jobs[job].hits[local] = h;
+      local = 0xFFFFFFFFu;
+    }
+  }
+}
+
+using PoolKernel = void (*)(DeviceScene, const DJob*, uint32_t*, int);
+
+struct PoolVariant {
+  int threads, minb;
+  PoolKernel k[2][2];  // [any][stack 192]
+  int bps[2][2];
+};
+
+template <int T, int M>
+PoolVariant make_pool_variant() {
+  PoolVariant v{T, M, {{k_pool_step<false, 64, T, M>, k_pool_step<false, 192, T, M>},
+                       {k_pool_step<true, 64, T, M>, k_pool_step<true, 192, T, M>}},
+                {{-1, -1}, {-1, -1}}};
+  return v;
+}
+
+PoolVariant g_pool_variants[] = {make_pool_variant<128, 12>(), make_pool_variant<128, 10>(),
+                                 make_pool_variant<128, 1>(), make_pool_variant<256, 6>()};
+constexpr int kNumPoolVariants = sizeof(g_pool_variants) / sizeof(g_pool_variants[0]);
+
+// First-fit range allocator over [0, capacity) with coalescing frees.
+class RangeAlloc {
+ public:
+  uint64_t capacity = 0;
+  std::map<uint64_t, uint64_t> free_;  // offset -> size
+  bool alloc(uint64_t n, uint64_t* off) {
+    if (n == 0) {
+      *off = 0;
+      return true;
+    }
+    for (auto it = free_.begin(); it != free_.end(); ++it) {
+      if (it->second >= n) {
+        *off = it->first;
+        const uint64_t rest = it->second - n, at = it->first + n;
+        free_.erase(it);
+        if (rest) free_[at] = rest;
+        return true;
+      }
+    }
+    return false;
+  }
+  void release(uint64_t off, uint64_t n) {
+    if (n == 0) return;
+    auto it = free_.emplace(off, n).first;
+    auto nx = std::next(it);
+    if (nx != free_.end() && it->first + it->second == nx->first) {
+      it->second += nx->second;
+      free_.erase(nx);
+    }
+    if (it != free_.begin()) {
+      auto pv = std::prev(it);
+      if (pv->first + pv->second == it->first) {
+        pv->second += it->second;
+        free_.erase(it);
+      }
+    }
+  }
+  void grow(uint64_t new_cap) {  // adds [capacity, new_cap) as free
+    const uint64_t old = capacity;
+    capacity = new_cap;
+    release(old, new_cap - old);
+  }
+};
+
+}  // namespace
+
+struct PoolScene {
+  uint32_t root = kSentinel;
+  uint64_t node_off = 0, node_cnt = 0;
+  uint64_t tri_off = 0, tri_cnt = 0;
+  uint64_t bytes = 0;
+  uint32_t stack_need = 1;
+  bool live = false;
+};
+
+struct LaunchSlot {
+  DJob* host = nullptr;   // pinned
+  DJob* dev = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  cudaGraph_t graph = nullptr;
+  cudaEvent_t done = nullptr;
+  bool used = false;
+  // what the graph was captured with
+  uint64_t generation = ~0ull;
+  int variant = -1, any = -1, big = -1, refill = -1;
+};
+
+struct StreamState {
+  uint32_t* counter = nullptr;
+  LaunchSlot slot[2];
+  int next = 0;
+};
+
+}  // namespace rtgb
+
+struct rt_pool {
+  std::mutex mu;
+  uint64_t budget = 0;
+  uint32_t max_scenes = 0;
+  uint64_t used = 0;
+  // arena
+  float4* inner = nullptr;
+  float4* tris = nullptr;
+  uint32_t* ids = nullptr;
+  rtgb::RangeAlloc nodes_alloc, tris_alloc;
+  uint64_t generation = 0;  // bumps whenever the arena arrays move
+  std::vector<rtgb::PoolScene> scenes;
+  uint32_t max_stack_need = 1;
+  int variant = 0;
+  int refill = 4;
+  std::unordered_map<cudaStream_t, rtgb::StreamState*> streams;
+};
+
+namespace rtgb {
+namespace {
+
+rt_status cuda_err(cudaError_t e, const char* what) {
+  set_error(std::string(what) + ": " + cudaGetErrorString(e));
+  return RT_ECUDA;
+}
+
+// Grows an arena array of `elem` bytes per entry from old_cap to new_cap entries.
+template <class T>
+cudaError_t grow_array(T** arr, uint64_t old_cap, uint64_t new_cap, size_t elem) {
+  void* p = nullptr;
+  cudaError_t e = cudaMalloc(&p, new_cap * elem);
+  if (e != cudaSuccess) return e;
+  if (*arr && old_cap) {
+    e = cudaMemcpy(p, *arr, old_cap * elem, cudaMemcpyDeviceToDevice);
+    if (e != cudaSuccess) {
+      cudaFree(p);
+      return e;
+    }
+  }
+  if (*arr) cudaFree(*arr);
+  *arr = static_cast<T*>(p);
+  return cudaSuccess;
+}
+
+DeviceScene arena_view(const rt_pool* P) {
+  DeviceScene d;
+  d.inner = P->inner;
+  d.tris = P->tris;
+  d.tri_ids = P->ids;
+  d.n_tris = (uint32_t)P->tris_alloc.capacity;
+  d.width = 4;
+  d.stack_need = P->max_stack_need;
+  return d;
+}
+
+StreamState* stream_state(rt_pool* P, cudaStream_t st, rt_status* status) {
+  auto it = P->streams.find(st);
+  if (it != P->streams.end()) return it->second;
+  std::unique_ptr<StreamState> ss(new StreamState());
+  cudaError_t e = cudaMalloc(&ss->counter, 256);
+  for (int i = 0; i < 2 && e == cudaSuccess; ++i) {
+    e = cudaMallocHost(&ss->slot[i].host, kTableBytes);
+    if (e == cudaSuccess) e = cudaMalloc(&ss->slot[i].dev, kTableBytes);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ss->slot[i].done, cudaEventDisableTiming);
+  }
+  if (e != cudaSuccess) {
+    *status = cuda_err(e, "rt_pool: stream state");
+    return nullptr;
+  }
+  StreamState* raw = ss.release();
+  P->streams[st] = raw;
+  return raw;
+}
+
+// Builds the job table in the slot's pinned buffer; returns the ray total.
+rt_status fill_table(rt_pool* P, const RtJob* jobs, uint32_t num_jobs, DJob* host, uint64_t* total_out) {
+  uint64_t total = 0;
+  DJob* out = host + 1;
+  for (uint32_t j = 0; j < num_jobs; ++j) {
+    const RtJob& J = jobs[j];
+    if (J.scene_id >= P->scenes.size() || !P->scenes[J.scene_id].live) {
+      set_error("rt_pool_trace: job " + std::to_string(j) + " names an unknown scene");
+      return RT_ENOTFOUND;
+    }
+    if (J.num_rays && (!J.d_rays || !J.d_hits)) {
+      set_error("rt_pool_trace: job " + std::to_string(j) + " has null ray/hit buffers");
+      return RT_EINVAL;
+    }
+    out[j].rays = reinterpret_cast<const float4*>(J.d_rays);
+    out[j].hits = reinterpret_cast<uint2*>(J.d_hits);
+    out[j].start = (uint32_t)total;
+    out[j].count = J.num_rays;
+    out[j].root = P->scenes[J.scene_id].root;
+    out[j].pad = 0;
+    total += J.num_rays;
+    if (total > 0x80000000ull) {
+      set_error("rt_pool_trace: more than 2^31 rays in one batch");
+      return RT_EINVAL;
+    }
+  }
+  uint32_t* hdr = reinterpret_cast<uint32_t*>(host);
+  std::memset(hdr, 0, sizeof(DJob));
+  hdr[0] = num_jobs;
+  hdr[1] = (uint32_t)total;
+  *total_out = total;
+  return RT_OK;
+}
+
+// Captures (table upload, queue reset, kernel) into the slot's graph.
+rt_status capture(rt_pool* P, LaunchSlot& sl, uint32_t* counter, int variant, int any, int big, int refill) {
+  if (sl.exec) cudaGraphExecDestroy(sl.exec);
+  if (sl.graph) cudaGraphDestroy(sl.graph);
+  sl.exec = nullptr;
+  sl.graph = nullptr;
+  PoolVariant& v = g_pool_variants[variant];
+  PoolKernel k = v.k[any][big];
+  int& bps = v.bps[any][big];
+  if (bps < 0) {
+    int b = 0;
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k, v.threads, 0);
+    if (e != cudaSuccess) return cuda_err(e, "rt_pool: occupancy");
+    bps = b < 1 ? 1 : b;
+  }
+  cudaStream_t cs;
+  cudaError_t e = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking);
+  if (e != cudaSuccess) return cuda_err(e, "rt_pool: capture stream");
+  e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(sl.dev, sl.host, kTableBytes, cudaMemcpyHostToDevice, cs);
+  if (e == cudaSuccess) e = cudaMemsetAsync(counter, 0, 8, cs);
+  if (e == cudaSuccess) {
+    const uint32_t blocks = (uint32_t)(device_sm_count() * bps);
+    k<<<blocks, v.threads, 0, cs>>>(arena_view(P), sl.dev, counter, refill);
+    e = cudaGetLastError();
+  }
+  cudaGraph_t g = nullptr;
+  cudaError_t e2 = cudaStreamEndCapture(cs, &g);
+  if (e == cudaSuccess) e = e2;
+  if (e == cudaSuccess) e = cudaGraphInstantiate(&sl.exec, g, 0);
+  sl.graph = g;
+  cudaStreamDestroy(cs);
+  if (e != cudaSuccess) return cuda_err(e, "rt_pool: graph capture");
+  sl.generation = P->generation;
+  sl.variant = variant;
+  sl.any = any;
+  sl.big = big;
+  sl.refill = refill;
+  return RT_OK;
+}
+
+rt_status pool_trace_locked(rt_pool* P, const RtJob* jobs, uint32_t num_jobs, uint32_t flags, cudaStream_t st,
+                            int variant, int refill) {
+  rt_status status = RT_OK;
+  StreamState* ss = stream_state(P, st, &status);
+  if (!ss) return status;
+  LaunchSlot& sl = ss->slot[ss->next];
+  ss->next ^= 1;
+  // the slot's pinned table may still be read by its previous launch
+  if (sl.used) {
+    cudaError_t e = cudaEventSynchronize(sl.done);
+    if (e != cudaSuccess) return cuda_err(e, "rt_pool_trace: slot wait");
+  }
+  uint64_t total = 0;
+  if ((status = fill_table(P, jobs, num_jobs, sl.host, &total)) != RT_OK) return status;
+  const int any = (flags & RT_TRACE_ANY) ? 1 : 0;
+  const int big = P->max_stack_need > 64u ? 1 : 0;
+  if (!sl.exec || sl.generation != P->generation || sl.variant != variant || sl.any != any || sl.big != big ||
+      sl.refill != refill) {
+    if ((status = capture(P, sl, ss->counter, variant, any, big, refill)) != RT_OK) return status;
+  }
+  cudaError_t e = cudaGraphLaunch(sl.exec, st);
+  if (e == cudaSuccess) e = cudaEventRecord(sl.done, st);
+  if (e != cudaSuccess) return cuda_err(e, "rt_pool_trace: graph launch");
+  sl.used = true;
+  return RT_OK;
+}
+
+}  // namespace
+
+// Rebases a converted scene's refs into the arena: inner refs by node_off,
+// triangle slots by tri_off (the count bits are kept).
+static void rebase(HostDeviceBVH& hb, uint32_t node_off, uint32_t tri_off) {
+  auto fix = [&](uint32_t r) -> uint32_t {
+    if (r == kSentinel) return r;
+    if (r < kSentinel) return r + node_off;
+    if (r & kSphereBit) return r;  // pools hold triangles only; unused slots stay empty
+    return (r & ~kSlotMask) | ((r & kSlotMask) + tri_off);
+  };
+  const size_t nn = hb.inner.size() / 16;
+  parallel_for(nn, [&](size_t b, size_t e, unsigned) {
+    for (size_t i = b; i < e; ++i)
+      for (int k = 4; k < 8; ++k) {
+        uint32_t u;
+        std::memcpy(&u, &hb.inner[16 * i + k], 4);
+        u = fix(u);
+        std::memcpy(&hb.inner[16 * i + k], &u, 4);
+      }
+  });
+  hb.root = fix(hb.root);
+}
+
+}  // namespace rtgb
+
+using namespace rtgb;
+
+extern "C" {
+
+rt_status rt_pool_create(const RtPoolOptions* opt, rt_pool** out) {
+  if (!out) {
+    set_error("rt_pool_create: null argument");
+    return RT_EINVAL;
+  }
+  *out = nullptr;
+  rt_pool* P = new rt_pool();
+  P->budget = (opt && opt->budget_bytes) ? opt->budget_bytes : (8ull << 30);
+  P->max_scenes = (opt && opt->max_scenes) ? opt->max_scenes : 4096u;
+  *out = P;
+  return RT_OK;
+}
+
+rt_status rt_pool_destroy(rt_pool* P) {
+  if (!P) return RT_OK;
+  cudaDeviceSynchronize();
+  for (auto& kv : P->streams) {
+    StreamState* ss = kv.second;
+    for (auto& sl : ss->slot) {
+      if (sl.exec) cudaGraphExecDestroy(sl.exec);
+      if (sl.graph) cudaGraphDestroy(sl.graph);
+      if (sl.host) cudaFreeHost(sl.host);
+      if (sl.dev) cudaFree(sl.dev);
+      if (sl.done) cudaEventDestroy(sl.done);
+    }
+    if (ss->counter) cudaFree(ss->counter);
+    delete ss;
+  }
+  if (P->inner) cudaFree(P->inner);
+  if (P->tris) cudaFree(P->tris);
+  if (P->ids) cudaFree(P->ids);
+  delete P;
+  return RT_OK;
+}
+
+rt_status rt_pool_add_scene(rt_pool* P, const RtSceneDesc* desc, uint32_t* out_id) {
+  if (!P || !desc || !out_id) {
+    set_error("rt_pool_add_scene: null argument");
+    return RT_EINVAL;
+  }
+  if (desc->num_spheres) {
+    set_error("rt_pool_add_scene: pooled scenes hold triangles only");
+    return RT_EUNSUPPORTED;
+  }
+  if (desc->num_triangles && !desc->triangles) {
+    set_error("rt_pool_add_scene: null triangles");
+    return RT_EINVAL;
+  }
+  if (desc->bvh_mode != RT_BVH_SORTED && desc->bvh_mode != RT_BVH_REFERENCE) {
+    set_error("rt_pool_add_scene: unknown bvh_mode");
+    return RT_EINVAL;
+  }
+  const uint32_t nt = desc->num_triangles;
+  if (desc->nodes && nt && desc->num_nodes != 2 * (uint64_t)nt - 1) {
+    set_error("rt_pool_add_scene: num_nodes must be 2*triangles-1");
+    return RT_EINVAL;
+  }
+  // Host work outside the lock: world space, BVH, device form.
+  std::vector<RtTriangle64> wt;
+  std::vector<RtSphere32> ws;
+  std::string msg;
+  if (!world_space(desc->triangles, nt, nullptr, 0, desc->models, desc->num_models, wt, ws, msg)) {
+    set_error("rt_pool_add_scene: " + msg);
+    return RT_EINVAL;
+  }
+  std::vector<RtBVHNode40> nodes;
+  if (desc->nodes)
+    nodes.assign(desc->nodes, desc->nodes + (nt ? 2 * (size_t)nt - 1 : 0));
+  else
+    build_bvh(wt.data(), nt, nullptr, 0, desc->bvh_mode, nodes);
+  HostDeviceBVH hb;
+  if (!convert_bvh(nodes.data(), (uint32_t)nodes.size(), wt.data(), nt, nullptr, 0, nullptr, 0, desc->leaf_size, 4, hb,
+                   msg)) {
+    set_error("rt_pool_add_scene: " + msg);
+    return RT_EINVAL;
+  }
+  if (hb.width != 4 || hb.stack_need > 192u) {
+    set_error("rt_pool_add_scene: BVH too deep for the pool's 4-wide traversal stack");
+    return RT_ESTACK;
+  }
+  const uint64_t n_nodes = hb.inner.size() / 16, n_tris = hb.tri_ids.size();
+  const uint64_t bytes = n_nodes * 64 + n_tris * 68;
+
+  std::lock_guard<std::mutex> lk(P->mu);
+  uint32_t live = 0;
+  for (auto& s : P->scenes) live += s.live ? 1u : 0u;
+  if (live >= P->max_scenes) {
+    set_error("rt_pool_add_scene: scene limit reached");
+    return RT_EBUSY;
+  }
+  if (P->used + bytes > P->budget) {
+    set_error("rt_pool_add_scene: " + std::to_string(bytes) + " bytes exceed the remaining budget of " +
+              std::to_string(P->budget - P->used));
+    return RT_ENOMEM;
+  }
+  uint64_t noff = 0, toff = 0;
+  bool moved = false;
+  while (!P->nodes_alloc.alloc(n_nodes, &noff)) {
+    const uint64_t cap = std::max<uint64_t>(2 * P->nodes_alloc.capacity, std::max<uint64_t>(n_nodes, 1u << 16));
+    if (cap >= kSentinel) {
+      set_error("rt_pool_add_scene: node arena full");
+      return RT_ENOMEM;
+    }
+    cudaDeviceSynchronize();  // no launch may read the arrays while they move
+    cudaError_t e = grow_array(&P->inner, P->nodes_alloc.capacity, cap, 64);
+    if (e != cudaSuccess) {
+      set_error(std::string("rt_pool_add_scene: node arena: ") + cudaGetErrorString(e));
+      return RT_ENOMEM;
+    }
+    P->nodes_alloc.grow(cap);
+    moved = true;
+  }
+  while (!P->tris_alloc.alloc(n_tris, &toff)) {
+    const uint64_t cap = std::min<uint64_t>(std::max<uint64_t>(2 * P->tris_alloc.capacity,
+                                                               std::max<uint64_t>(n_tris, 1u << 16)),
+                                            kMaxTriangles);
+    if (cap <= P->tris_alloc.capacity) {
+      P->nodes_alloc.release(noff, n_nodes);
+      set_error("rt_pool_add_scene: triangle arena full (2^27 triangles)");
+      return RT_ENOMEM;
+    }
+    cudaDeviceSynchronize();
+    cudaError_t e = grow_array(&P->tris, P->tris_alloc.capacity, cap, 64);
+    if (e == cudaSuccess) e = grow_array(&P->ids, P->tris_alloc.capacity, cap, 4);
+    if (e != cudaSuccess) {
+      P->nodes_alloc.release(noff, n_nodes);
+      set_error(std::string("rt_pool_add_scene: triangle arena: ") + cudaGetErrorString(e));
+      return RT_ENOMEM;
+    }
+    P->tris_alloc.grow(cap);
+    moved = true;
+  }
+  if (moved) P->generation++;
+  rebase(hb, (uint32_t)noff, (uint32_t)toff);
+  cudaError_t e = cudaSuccess;
+  if (n_nodes) e = cudaMemcpy(P->inner + 4 * noff, hb.inner.data(), n_nodes * 64, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess && n_tris) e = cudaMemcpy(P->tris + 4 * toff, hb.tris.data(), n_tris * 64, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess && n_tris) e = cudaMemcpy(P->ids + toff, hb.tri_ids.data(), n_tris * 4, cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) {
+    P->nodes_alloc.release(noff, n_nodes);
+    P->tris_alloc.release(toff, n_tris);
+    return cuda_err(e, "rt_pool_add_scene: upload");
+  }
+  PoolScene ps;
+  ps.root = hb.root;
+  ps.node_off = noff;
+  ps.node_cnt = n_nodes;
+  ps.tri_off = toff;
+  ps.tri_cnt = n_tris;
+  ps.bytes = bytes;
+  ps.stack_need = hb.stack_need;
+  ps.live = true;
+  uint32_t id = (uint32_t)P->scenes.size();
+  for (uint32_t i = 0; i < P->scenes.size(); ++i)
+    if (!P->scenes[i].live) {
+      id = i;
+      break;
+    }
+  if (id == P->scenes.size()) P->scenes.push_back(ps);
+  else P->scenes[id] = ps;
+  P->used += bytes;
+  if (hb.stack_need > P->max_stack_need) P->max_stack_need = hb.stack_need;
+  *out_id = id;
+  return RT_OK;
+}
+
+rt_status rt_pool_remove_scene(rt_pool* P, uint32_t id) {
+  if (!P) return RT_EINVAL;
+  std::lock_guard<std::mutex> lk(P->mu);
+  if (id >= P->scenes.size() || !P->scenes[id].live) {
+    set_error("rt_pool_remove_scene: unknown scene");
+    return RT_ENOTFOUND;
+  }
+  PoolScene& s = P->scenes[id];
+  P->nodes_alloc.release(s.node_off, s.node_cnt);
+  P->tris_alloc.release(s.tri_off, s.tri_cnt);
+  P->used -= s.bytes;
+  s = PoolScene();
+  return RT_OK;
+}
+
+rt_status rt_pool_get_info(const rt_pool* Pc, RtPoolInfo* out) {
+  if (!Pc || !out) return RT_EINVAL;
+  rt_pool* P = const_cast<rt_pool*>(Pc);
+  std::lock_guard<std::mutex> lk(P->mu);
+  std::memset(out, 0, sizeof(*out));
+  uint64_t tris = 0;
+  for (auto& s : P->scenes)
+    if (s.live) {
+      out->num_scenes++;
+      tris += s.tri_cnt;
+    }
+  out->stack_need = P->max_stack_need;
+  out->used_bytes = P->used;
+  out->budget_bytes = P->budget;
+  out->arena_bytes = P->nodes_alloc.capacity * 64 + P->tris_alloc.capacity * 68;
+  out->num_triangles = (uint32_t)tris;
+  out->tuned_variant = (uint32_t)P->variant;
+  out->tuned_refill = P->refill;
+  return RT_OK;
+}
+
+rt_status rt_pool_trace(rt_pool* P, const RtJob* jobs, uint32_t num_jobs, uint32_t flags, void* stream) {
+  if (!P || (num_jobs && !jobs) || num_jobs > kMaxJobs || flags > RT_TRACE_ANY) {
+    set_error("rt_pool_trace: bad argument (at most 8192 jobs; flags closest or any)");
+    return RT_EINVAL;
+  }
+  std::lock_guard<std::mutex> lk(P->mu);
+  return pool_trace_locked(P, jobs, num_jobs, flags, reinterpret_cast<cudaStream_t>(stream), P->variant, P->refill);
+}
+
+rt_status rt_pool_autotune(rt_pool* P, const RtJob* jobs, uint32_t num_jobs, uint32_t flags, void* stream,
+                           uint32_t repeats) {
+  if (!P || (num_jobs && !jobs) || num_jobs > kMaxJobs || flags > RT_TRACE_ANY) {
+    set_error("rt_pool_autotune: bad argument");
+    return RT_EINVAL;
+  }
+  if (repeats == 0) repeats = 3;
+  std::lock_guard<std::mutex> lk(P->mu);
+  cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+  static const int refills[] = {1, 4, 8, 16};
+  cudaEvent_t a, b;
+  cudaEventCreate(&a);
+  cudaEventCreate(&b);
+  float best = 3.4e38f;
+  int bv = P->variant, br = P->refill;
+  rt_status status = RT_OK;
+  for (int v = 0; v < kNumPoolVariants && status == RT_OK; ++v)
+    for (int r : refills) {
+      // warm-up: captures the graphs of both launch slots outside the timing
+      if ((status = pool_trace_locked(P, jobs, num_jobs, flags, st, v, r)) != RT_OK) break;
+      if ((status = pool_trace_locked(P, jobs, num_jobs, flags, st, v, r)) != RT_OK) break;
+      cudaEventRecord(a, st);
+      for (uint32_t k = 0; k < repeats && status == RT_OK; ++k) status = pool_trace_locked(P, jobs, num_jobs, flags, st, v, r);
+      cudaEventRecord(b, st);
+      if (cudaEventSynchronize(b) != cudaSuccess) {
+        status = cuda_err(cudaGetLastError(), "rt_pool_autotune");
+        break;
+      }
+      float ms = 0.0f;
+      cudaEventElapsedTime(&ms, a, b);
+      if (ms < best) {
+        best = ms;
+        bv = v;
+        br = r;
+      }
+    }
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  if (status != RT_OK) return status;
+  P->variant = bv;
+  P->refill = br;
+  return RT_OK;
+}
+
+rt_status rt_pool_describe_variant(uint32_t v, uint32_t* threads, uint32_t* min_blocks) {
+  if (v >= (uint32_t)kNumPoolVariants || !threads || !min_blocks) return RT_EINVAL;
+  *threads = (uint32_t)g_pool_variants[v].threads;
+  *min_blocks = (uint32_t)g_pool_variants[v].minb;
+  return RT_OK;
+}
+
+}  // extern "C"

@@ -179,3 +179,21 @@ def test_library_refuses_to_load_when_missing(tmp_path):
             "try:\n    rt.lib()\nexcept ImportError as e:\n    print('refused', e)\n") % (str(tmp_path / "none.so"), str(ROOT))
     r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True)
     assert "refused" in r.stdout
+
+
+def test_pool_admission_without_a_gpu(rt):
+    """Admission and validation happen before any device work."""
+    soup = rt.gen_soup(8, 0, 20_000)
+    with rt.Pool(budget_bytes=1000) as pool:
+        with pytest.raises(rt.RtError) as e:
+            pool.add_scene(soup)
+        assert e.value.status == 2 and "budget" in str(e.value)
+        assert pool.info().num_scenes == 0 and pool.info().used_bytes == 0
+    with rt.Pool() as pool:
+        with pytest.raises(rt.RtError) as e:
+            pool.add_scene(soup, bvh_mode=5)
+        assert e.value.status == 1
+        with pytest.raises(rt.RtError) as e:
+            pool.trace([(0, None, None, 0)] * 9000)
+        assert e.value.status == 1
+    assert rt.describe_pool_variant(0) == (128, 12)

@@ -1,0 +1,96 @@
+"""GPU tests of the scene pool (rt_pool_*): one launch over many scenes must
+return exactly what rt_trace returns on each scene alone."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def soups(rt, seed, count, lo=1_000, hi=60_000):
+    u = rt.gen_uniform(seed, 99, 2 * count)
+    out = []
+    for i in range(count):
+        nt = int(round(np.exp(np.log(lo) + (np.log(hi) - np.log(lo)) * u[2 * i])))
+        nr = int(round(np.exp(np.log(2_000) + (np.log(80_000) - np.log(2_000)) * u[2 * i + 1])))
+        side = (nt / 4_194_304) ** (1 / 3)
+        out.append((rt.gen_soup(seed, i + 1, nt, side, 0.002), rt.gen_rays(seed, i + 1, nr, side, 1e-4, float("inf"))))
+    return out
+
+
+def alone(rt, torch, tris, rays, any_hit=False):
+    with rt.Scene(tris) as sc:
+        d_rays = torch.from_numpy(rays.view(np.uint8)).cuda()
+        d_hits = torch.empty(len(rays) * 8, dtype=torch.uint8, device="cuda")
+        sc.trace(d_rays, d_hits, any_hit=any_hit)
+        torch.cuda.synchronize()
+        return d_hits.cpu().numpy().view(rt.HIT_DTYPE)
+
+
+def run_pool(rt, torch, pool, ids, data, any_hit=False, autotune=False):
+    dr = [torch.from_numpy(r.view(np.uint8)).cuda() for _, r in data]
+    dh = [torch.full((len(r) * 8,), 0xEE, dtype=torch.uint8, device="cuda") for _, r in data]
+    jobs = [(sid, a, b) for sid, a, b in zip(ids, dr, dh)]
+    if autotune:
+        pool.autotune(jobs, any_hit=any_hit, repeats=1)
+    pool.trace(jobs, any_hit=any_hit)
+    torch.cuda.synchronize()
+    return [h.cpu().numpy().view(rt.HIT_DTYPE) for h in dh]
+
+
+def test_pool_matches_individual_scenes(rt, cuda):
+    data = soups(rt, 41, 24)
+    with rt.Pool() as pool:
+        ids = [pool.add_scene(t) for t, _ in data]
+        assert pool.info().num_scenes == 24
+        for anyh in (False, True):
+            got = run_pool(rt, cuda, pool, ids, data, any_hit=anyh)
+            for (t, r), g in zip(data, got):
+                assert np.array_equal(g.view(np.uint64), alone(rt, cuda, t, r, any_hit=anyh).view(np.uint64))
+        # a second launch on the same stream (other launch slot) and an autotuned one
+        got = run_pool(rt, cuda, pool, ids[::-1], data[::-1], autotune=True)
+        for (t, r), g in zip(data[::-1], got):
+            assert np.array_equal(g.view(np.uint64), alone(rt, cuda, t, r).view(np.uint64))
+
+
+def test_pool_remove_reuse_and_growth(rt, cuda):
+    data = soups(rt, 42, 40, lo=20_000, hi=120_000)
+    with rt.Pool() as pool:
+        ids = [pool.add_scene(t) for t, _ in data[:10]]
+        arena0 = pool.info().arena_bytes
+        for k in (1, 4, 7):
+            pool.remove_scene(ids[k])
+        with pytest.raises(rt.RtError) as e:
+            pool.remove_scene(ids[4])
+        assert e.value.status == 8  # RT_ENOTFOUND
+        more = [pool.add_scene(t) for t, _ in data[10:]]  # fills the holes, then grows the arena
+        assert pool.info().arena_bytes > arena0
+        keep = [i for i in range(10) if i not in (1, 4, 7)]
+        sel_ids = [ids[i] for i in keep] + more
+        sel = [data[i] for i in keep] + data[10:]
+        got = run_pool(rt, cuda, pool, sel_ids, sel)
+        for (t, r), g in zip(sel, got):
+            assert np.array_equal(g.view(np.uint64), alone(rt, cuda, t, r).view(np.uint64))
+
+
+def test_pool_budget_and_empty_jobs(rt, cuda):
+    data = soups(rt, 43, 3, lo=50_000, hi=50_001)
+    with rt.Pool(budget_bytes=9_000_000) as pool:
+        a = pool.add_scene(data[0][0])
+        with pytest.raises(rt.RtError) as e:
+            pool.add_scene(data[1][0])
+            pool.add_scene(data[2][0])
+        assert e.value.status == 2  # RT_ENOMEM
+        used = pool.info().used_bytes
+        assert used <= 9_000_000
+        pool.remove_scene(a)
+        b = pool.add_scene(data[1][0])
+        t, r = data[1]
+        zero = cuda.empty(8, dtype=cuda.uint8, device="cuda")
+        d_rays = cuda.from_numpy(r.view(np.uint8)).cuda()
+        d_hits = cuda.empty(len(r) * 8, dtype=cuda.uint8, device="cuda")
+        pool.trace([(b, zero, zero, 0), (b, d_rays, d_hits), (b, zero, zero, 0)])
+        cuda.cuda.synchronize()
+        assert np.array_equal(d_hits.cpu().numpy().view(np.uint64), alone(rt, cuda, t, r).view(np.uint64))
+        pool.trace([])
+        with pytest.raises(rt.RtError):
+            pool.trace([(999, d_rays, d_hits)])
