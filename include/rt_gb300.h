@@ -310,6 +310,67 @@ rt_status rt_pool_autotune(rt_pool* pool, const RtJob* jobs, uint32_t num_jobs, 
                            uint32_t repeats);
 rt_status rt_pool_describe_variant(uint32_t variant, uint32_t* threads, uint32_t* min_blocks);
 
+/* ---------------------------------------------------------------- serving */
+/* A request loop over a scene pool (no counterpart in the reference): keeps
+ * scenes resident on the device, admits ray queries and scene uploads, and
+ * batches queries continuously -- queries that arrive while earlier batches
+ * run are staged and launched on further streams (up to max_inflight batches
+ * on the device at once) as staging memory frees up.  Uploads are admitted
+ * against the byte budget, evicting least-recently-used idle scenes.
+ * Host ray/hit buffers and upload arrays must stay valid until the request
+ * completes; pinned host memory lets the copies run asynchronously. */
+typedef struct rt_server rt_server;
+
+typedef struct RtServerOptions {
+  uint64_t budget_bytes;    /* resident scene bytes; 0 = 8 GiB */
+  uint32_t max_scenes;      /* 0 = 4096 */
+  uint32_t stage_rays;      /* device staging capacity in rays (40 B each); 0 = 2^25 */
+  uint32_t max_batch_rays;  /* rays per batch launch; 0 = 2^23 */
+  uint32_t max_batch_jobs;  /* queries per batch launch (<= 8192); 0 = 1024 */
+  uint32_t max_inflight;    /* batches on the device at once (<= 16); 0 = 3 */
+  uint32_t _pad;
+} RtServerOptions;
+
+typedef struct RtServerStats {
+  uint64_t requests_done;
+  uint64_t rays_done;
+  uint64_t uploads_done;
+  uint64_t batches;
+  uint64_t evictions;
+  uint32_t pending;
+  uint32_t inflight_batches;
+  uint32_t resident_scenes;
+  uint32_t _pad;
+  uint64_t resident_bytes;
+} RtServerStats;
+
+typedef struct RtRequestResult {
+  int32_t status;           /* rt_status of the request */
+  uint32_t scene_id;        /* the query's scene, or the id an upload received */
+  uint32_t num_rays;
+  uint32_t batch_jobs;      /* queries in the batch that carried this one */
+  double latency_seconds;   /* submit -> completion */
+  double queue_seconds;     /* submit -> start */
+} RtRequestResult;
+
+rt_status rt_server_create(const RtServerOptions* opt, rt_server** out_server);
+/* Cancels queued requests, waits for running ones, frees everything. */
+rt_status rt_server_destroy(rt_server* server);
+/* Queues a scene upload (BVH built on the host by the server). */
+rt_status rt_server_upload(rt_server* server, const RtSceneDesc* desc, uint64_t* out_request);
+/* Queues a closest/any-hit query of n host rays into host hits. */
+rt_status rt_server_submit(rt_server* server, uint32_t scene_id, const RtRay* h_rays, uint32_t n, RtHit* h_hits,
+                           uint32_t flags, uint64_t* out_request);
+/* Cancels a request that has not started (RT_EBUSY once it runs). */
+rt_status rt_server_cancel(rt_server* server, uint64_t request);
+/* Waits up to timeout_seconds; RT_ETIMEOUT leaves the request queryable.
+ * Returns the request's status and forgets it. */
+rt_status rt_server_wait(rt_server* server, uint64_t request, double timeout_seconds, RtRequestResult* out);
+rt_status rt_server_remove_scene(rt_server* server, uint32_t scene_id);
+rt_status rt_server_get_stats(rt_server* server, RtServerStats* out);
+/* Runs the pool autotuner on one resident scene's device ray batch. */
+rt_status rt_server_autotune(rt_server* server, uint32_t scene_id, const RtRay* d_rays, uint32_t n, RtHit* d_hits);
+
 /* ----------------------------------------------------------------- render */
 enum {
   RT_SHADE_REFERENCE = 0, /* LIGHT emits, DIFFUSE scatters, others terminate, background 0 */

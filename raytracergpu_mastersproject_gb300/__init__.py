@@ -97,6 +97,24 @@ class Job(C.Structure):
     _fields_ = [("scene_id", C.c_uint32), ("num_rays", C.c_uint32), ("d_rays", C.c_void_p), ("d_hits", C.c_void_p)]
 
 
+class ServerOptions(C.Structure):
+    _fields_ = [("budget_bytes", C.c_uint64), ("max_scenes", C.c_uint32), ("stage_rays", C.c_uint32),
+                ("max_batch_rays", C.c_uint32), ("max_batch_jobs", C.c_uint32), ("max_inflight", C.c_uint32),
+                ("_pad", C.c_uint32)]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [("requests_done", C.c_uint64), ("rays_done", C.c_uint64), ("uploads_done", C.c_uint64),
+                ("batches", C.c_uint64), ("evictions", C.c_uint64), ("pending", C.c_uint32),
+                ("inflight_batches", C.c_uint32), ("resident_scenes", C.c_uint32), ("_pad", C.c_uint32),
+                ("resident_bytes", C.c_uint64)]
+
+
+class RequestResult(C.Structure):
+    _fields_ = [("status", C.c_int32), ("scene_id", C.c_uint32), ("num_rays", C.c_uint32),
+                ("batch_jobs", C.c_uint32), ("latency_seconds", C.c_double), ("queue_seconds", C.c_double)]
+
+
 class _RenderOptions(C.Structure):
     _fields_ = [("shade_mode", C.c_uint32), ("background", C.c_float * 3)]
 
@@ -132,6 +150,15 @@ SIGNATURES = {
     "rt_pool_trace": (_I, [_P, C.POINTER(Job), _U32, _U32, _P]),
     "rt_pool_autotune": (_I, [_P, C.POINTER(Job), _U32, _U32, _P, _U32]),
     "rt_pool_describe_variant": (_I, [_U32, C.POINTER(_U32), C.POINTER(_U32)]),
+    "rt_server_create": (_I, [C.POINTER(ServerOptions), C.POINTER(C.c_void_p)]),
+    "rt_server_destroy": (_I, [_P]),
+    "rt_server_upload": (_I, [_P, C.POINTER(_SceneDesc), C.POINTER(_U64)]),
+    "rt_server_submit": (_I, [_P, _U32, _P, _U32, _P, _U32, C.POINTER(_U64)]),
+    "rt_server_cancel": (_I, [_P, _U64]),
+    "rt_server_wait": (_I, [_P, _U64, _D, C.POINTER(RequestResult)]),
+    "rt_server_remove_scene": (_I, [_P, _U32]),
+    "rt_server_get_stats": (_I, [_P, C.POINTER(ServerStats)]),
+    "rt_server_autotune": (_I, [_P, _U32, _P, _U32, _P]),
     "rt_gen_uniform": (_I, [_U64, _U64, _U64, _P]),
     "rt_gen_icosphere": (_I, [_U32, _P, _F, _U32, _P, _U64, C.POINTER(_U64)]),
     "rt_gen_config1": (_I, [_P, C.POINTER(RaytracingUBO), _P]),
@@ -359,6 +386,91 @@ class Pool:
         if getattr(self, "_h", None) is not None and self._h.value:
             lib().rt_pool_destroy(self._h.value)
         self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+
+class Server:
+    """Serving loop over resident scenes (rt_server_*).
+
+    upload() and submit() queue requests and return their ids at once; wait()
+    returns the RequestResult (status, latency, batch size) and raises on an
+    error status.  Host arrays handed to upload()/submit() are kept alive here
+    until their request is waited for."""
+
+    def __init__(self, budget_bytes: int = 0, max_scenes: int = 0, stage_rays: int = 0, max_batch_rays: int = 0,
+                 max_batch_jobs: int = 0, max_inflight: int = 0):
+        opt = ServerOptions(budget_bytes, max_scenes, stage_rays, max_batch_rays, max_batch_jobs, max_inflight, 0)
+        h = C.c_void_p()
+        _check(lib().rt_server_create(C.byref(opt), C.byref(h)), "rt_server_create")
+        self._h = h
+        self._keep = {}
+
+    @property
+    def handle(self) -> int:
+        if self._h is None:
+            raise ValueError("server destroyed")
+        return self._h.value
+
+    def upload(self, triangles, models=None, bvh_mode: int = BVH_SORTED) -> int:
+        d, keep = _desc(triangles, models, None, bvh_mode, 0, 4)
+        rid = C.c_uint64()
+        _check(lib().rt_server_upload(self.handle, C.byref(d), C.byref(rid)), "rt_server_upload")
+        self._keep[rid.value] = (d, keep)
+        return rid.value
+
+    def submit(self, scene_id: int, rays: np.ndarray, hits: np.ndarray | None = None, any_hit: bool = False) -> int:
+        """rays/hits: host arrays (pinned memory makes the copies asynchronous)."""
+        if hits is None:
+            hits = np.empty(len(rays), HIT_DTYPE)
+        rid = C.c_uint64()
+        _check(lib().rt_server_submit(self.handle, scene_id, _ptr(rays), len(rays), _ptr(hits),
+                                      TRACE_ANY if any_hit else TRACE_CLOSEST, C.byref(rid)), "rt_server_submit")
+        self._keep[rid.value] = (rays, hits)
+        return rid.value
+
+    def hits(self, request_id: int):
+        return self._keep[request_id][1]
+
+    def cancel(self, request_id: int) -> None:
+        _check(lib().rt_server_cancel(self.handle, request_id), "rt_server_cancel")
+
+    def wait(self, request_id: int, timeout: float = 60.0) -> RequestResult:
+        res = RequestResult()
+        st = lib().rt_server_wait(self.handle, request_id, timeout, C.byref(res))
+        if st != 3:  # RT_ETIMEOUT keeps the request (and its arrays) alive
+            self._keep.pop(request_id, None)
+        _check(st, "rt_server_wait")
+        return res
+
+    def remove_scene(self, scene_id: int) -> None:
+        _check(lib().rt_server_remove_scene(self.handle, scene_id), "rt_server_remove_scene")
+
+    def stats(self) -> ServerStats:
+        st = ServerStats()
+        _check(lib().rt_server_get_stats(self.handle, C.byref(st)), "rt_server_get_stats")
+        return st
+
+    def autotune(self, scene_id: int, d_rays, d_hits, n: int | None = None) -> None:
+        if n is None:
+            n = d_rays.numel() * d_rays.element_size() // RAY_DTYPE.itemsize
+        _check(lib().rt_server_autotune(self.handle, scene_id, _ptr(d_rays), n, _ptr(d_hits)), "rt_server_autotune")
+
+    def close(self) -> None:
+        if getattr(self, "_h", None) is not None and self._h.value:
+            lib().rt_server_destroy(self._h.value)
+        self._h = None
+        self._keep = {}
 
     def __del__(self):
         try:
