@@ -60,6 +60,10 @@ def parse():
     p.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-sort", action="store_true", help="trace in the given ray order (no RT_TRACE_SORT)")
+    p.add_argument("--no-batched", action="store_true", help="skip the config-4 batched comparison")
+    p.add_argument("--no-served", action="store_true", help="skip the config-5 serving run")
+    p.add_argument("--serve-requests", type=int, default=200)
+    p.add_argument("--serve-rates", type=str, default="1000,4000,8000", help="Poisson arrival rates (requests/s)")
     return p.parse_args()
 
 
@@ -166,6 +170,141 @@ def cpu_leg(tris, nodes, rays, sample: int) -> tuple[dict, dict]:
             "sample": f"first {len(sub)} rays of the config-3 batch, oracle restatement of hitBVH "
                       f"(reference order, no culling, sorted-leaf BVH), {cores} threads, {dt:.2f} s"}
     return base, {"counts": counts, "ref_hits": ref_hits, "can_hits": can_hits}
+
+
+def _time_events(torch, fn, warmup: int = 2, reps: int = 5) -> float:
+    for _ in range(warmup):
+        fn()
+    torch.cuda.synchronize()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record()
+    for _ in range(reps):
+        fn()
+    b.record()
+    torch.cuda.synchronize()
+    return a.elapsed_time(b) / reps
+
+
+def run_batched(torch, rt) -> dict:
+    """Config 4: 256 soups with their own ray batches -- 256 plain rt_trace
+    calls vs one autotuned pool launch replayed from a CUDA graph."""
+    from raytracergpu_mastersproject_gb300 import workloads as wl
+
+    data = wl.config4()
+    nt = int(sum(len(t) for t, _ in data))
+    nr = int(sum(len(r) for _, r in data))
+    scenes = [rt.Scene(t) for t, _ in data]
+    pool = rt.Pool(budget_bytes=32 << 30)
+    ids = [pool.add_scene(t) for t, _ in data]
+    dr = [torch.from_numpy(r.view(np.uint8)).cuda() for _, r in data]
+    dh_plain = [torch.empty(len(r) * 8, dtype=torch.uint8, device="cuda") for _, r in data]
+    dh_batch = [torch.empty(len(r) * 8, dtype=torch.uint8, device="cuda") for _, r in data]
+    jobs = list(zip(ids, dr, dh_batch))
+
+    def plain():
+        for sc, a, b in zip(scenes, dr, dh_plain):
+            sc.trace(a, b)
+
+    def batched():
+        pool.trace(jobs)
+
+    ms_plain = _time_events(torch, plain)
+    ms_untuned = _time_events(torch, batched)
+    variant, refill = pool.autotune(jobs, repeats=2)
+    ms_batch = _time_events(torch, batched)
+    plain()
+    batched()
+    torch.cuda.synchronize()
+    same = all(torch.equal(a, b) for a, b in zip(dh_plain, dh_batch))
+    thr, minb = rt.describe_pool_variant(variant)
+    out = {"workload": "config 4: 256 triangle soups, counts log-uniform in [1K, 256K], each with a ray batch "
+                       "log-uniform in [4K, 1M] rays, closest-hit",
+           "triangles": nt, "rays": nr, "unit": UNIT,
+           "plain": {"value": nr / ms_plain / 1e6, "ms": ms_plain, "launches": 256,
+                     "path": "one rt_trace per scene"},
+           "batched": {"value": nr / ms_batch / 1e6, "ms": ms_batch, "launches": 1, "cuda_graph": True,
+                       "untuned_ms": ms_untuned,
+                       "autotuned": {"threads_per_block": thr, "min_blocks_per_sm": minb, "refill": refill}},
+           "speedup": ms_plain / ms_batch, "identical_hits": bool(same)}
+    pool.close()
+    for sc in scenes:
+        sc.close()
+    return out
+
+
+def run_served(torch, rt, n_requests: int, rates: list[float]) -> dict:
+    """Config 5: 64 resident scenes, Poisson arrivals; 90% ray queries
+    (log-uniform [1K, 2M] rays, closest-hit), 10% new-scene uploads; latency
+    p50/p99 and rays/s with continuous batching vs plain sequential service."""
+    from raytracergpu_mastersproject_gb300 import workloads as wl
+
+    n_scenes = 64
+    t0 = time.perf_counter()
+    resident = [wl.config5_scene(i) for i in range(n_scenes)]
+    ray_pool_t = torch.from_numpy(rt.gen_rays(5, 0, 2_000_000, 1.0, 1e-4, float("inf")).view(np.uint8)).pin_memory()
+    ray_pool = ray_pool_t.numpy().view(rt.RAY_DTYPE)
+    srv = rt.Server(budget_bytes=150 << 30, max_inflight=3, max_batch_rays=1 << 23)
+    sids = [srv.wait(srv.upload(t), 600.0).scene_id for t in resident]
+    setup_s = time.perf_counter() - t0
+    res_tris = int(sum(len(t) for t in resident))
+    runs = []
+    for ri, rate in enumerate(rates):
+        reqs = wl.config5_requests(n_requests, rate, n_scenes, seed_stream=ri)
+        uploads = [wl.config5_scene(1000 + 100 * ri + k) for k in range(sum(1 for r in reqs if r[1] == "upload"))]
+        tot_rays = sum(r[3] for r in reqs)
+        hits_t = torch.empty(max(tot_rays, 1) * 8, dtype=torch.uint8).pin_memory()
+        hits = hits_t.numpy().view(rt.HIT_DTYPE)
+        entry = {"rate_per_s": rate, "requests": n_requests, "ray_requests": sum(1 for r in reqs if r[1] == "rays"),
+                 "uploads": len(uploads), "rays": tot_rays}
+        for mode in ("batched", "sequential"):
+            if mode == "batched":
+                srv.set_batching(1024, 3)
+            else:
+                srv.set_batching(1, 1)
+            ids, kinds, new_scenes = [], [], []
+            hoff = 0
+            start = time.perf_counter()
+            for (t_arr, kind, idx, n, off) in reqs:
+                delay = start + t_arr - time.perf_counter()
+                if delay > 0:
+                    time.sleep(delay)
+                if kind == "upload":
+                    ids.append(srv.upload(uploads[idx]))
+                else:
+                    ids.append(srv.submit(sids[idx], ray_pool[off:off + n], hits[hoff:hoff + n]))
+                    hoff += n
+                kinds.append(kind)
+            lat, up_lat, batch_jobs = [], [], []
+            first_arr, last_done = None, 0.0
+            for rid, kind, rq in zip(ids, kinds, reqs):
+                r = srv.wait(rid, 600.0)
+                if kind == "rays":
+                    lat.append(r.latency_seconds)
+                    batch_jobs.append(r.batch_jobs)
+                    first_arr = rq[0] if first_arr is None else min(first_arr, rq[0])
+                    last_done = max(last_done, rq[0] + r.latency_seconds)
+                else:
+                    up_lat.append(r.latency_seconds)
+                    new_scenes.append(r.scene_id)
+            wall = max(last_done - (first_arr or 0.0), 1e-9)  # span of the ray queries
+            for sid in new_scenes:
+                srv.remove_scene(sid)
+            lat_ms = np.array(lat) * 1e3
+            entry[mode] = {"p50_ms": float(np.percentile(lat_ms, 50)), "p99_ms": float(np.percentile(lat_ms, 99)),
+                           "mean_ms": float(lat_ms.mean()), "rays_per_s": tot_rays / wall,
+                           "Grays_per_s": tot_rays / wall / 1e9, "query_span_s": wall,
+                           "mean_queries_per_launch": float(np.mean(batch_jobs)),
+                           "upload_p50_s": float(np.median(up_lat)) if up_lat else None}
+        runs.append(entry)
+    st = srv.stats()
+    srv.close()
+    return {"workload": "config 5: 64 resident soups (counts log-uniform in [64K, 4M]), Poisson arrivals, "
+                        "90% closest-hit queries of log-uniform [1K, 2M] rays from pinned host memory, "
+                        "10% new-scene uploads; HBM budget 150 GB",
+            "resident_triangles": res_tris, "setup_s": setup_s, "runs": runs,
+            "batches_total": int(st.batches), "evictions": int(st.evictions),
+            "latency": "submit of the host request to its hits back in host memory",
+            "sequential": "same server, one query per launch, one launch at a time"}
 
 
 def run_reference(args):
@@ -286,6 +425,9 @@ def run_ours(args):
 
     if rank != 0:
         return
+    batched = None if args.no_batched else run_batched(torch, rt)
+    served = None if args.no_served else run_served(
+        torch, rt, args.serve_requests, [float(x) for x in args.serve_rates.split(",") if x])
     peak, peak_kind = measured_peak()
     cpu_base, counts, parity = None, None, None
     if not args.no_cpu:
@@ -322,6 +464,7 @@ def run_ours(args):
                        "ray_order": "origin-bucketed inside the step (RT_TRACE_SORT)" if sort else "as given",
                        "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU"},
             "roofline": roof, "cpu_baseline": cpu_base, "e2e": e2e, "clocks": clk,
+            "batched": batched, "served": served,
             "gpu_launches": args.steps * (4 if sort else 1), "parity_sample": parity,
             "scene_build_s": info.build_seconds}
     print(json.dumps(line), flush=True)

@@ -368,6 +368,10 @@ rt_status rt_server_cancel(rt_server* server, uint64_t request);
 rt_status rt_server_wait(rt_server* server, uint64_t request, double timeout_seconds, RtRequestResult* out);
 rt_status rt_server_remove_scene(rt_server* server, uint32_t scene_id);
 rt_status rt_server_get_stats(rt_server* server, RtServerStats* out);
+/* Changes the batching policy of a running server: queries per launch and
+ * batches on the device at once (at most the max_inflight it was created with).
+ * max_batch_jobs = max_inflight = 1 gives plain sequential service. */
+rt_status rt_server_set_batching(rt_server* server, uint32_t max_batch_jobs, uint32_t max_inflight);
 /* Runs the pool autotuner on one resident scene's device ray batch. */
 rt_status rt_server_autotune(rt_server* server, uint32_t scene_id, const RtRay* d_rays, uint32_t n, RtHit* d_hits);
 

@@ -159,6 +159,7 @@ SIGNATURES = {
     "rt_server_remove_scene": (_I, [_P, _U32]),
     "rt_server_get_stats": (_I, [_P, C.POINTER(ServerStats)]),
     "rt_server_autotune": (_I, [_P, _U32, _P, _U32, _P]),
+    "rt_server_set_batching": (_I, [_P, _U32, _U32]),
     "rt_gen_uniform": (_I, [_U64, _U64, _U64, _P]),
     "rt_gen_icosphere": (_I, [_U32, _P, _F, _U32, _P, _U64, C.POINTER(_U64)]),
     "rt_gen_config1": (_I, [_P, C.POINTER(RaytracingUBO), _P]),
@@ -455,6 +456,9 @@ class Server:
 
     def remove_scene(self, scene_id: int) -> None:
         _check(lib().rt_server_remove_scene(self.handle, scene_id), "rt_server_remove_scene")
+
+    def set_batching(self, max_batch_jobs: int, max_inflight: int) -> None:
+        _check(lib().rt_server_set_batching(self.handle, max_batch_jobs, max_inflight), "rt_server_set_batching")
 
     def stats(self) -> ServerStats:
         st = ServerStats()

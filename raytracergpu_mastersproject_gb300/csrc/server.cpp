@@ -482,6 +482,18 @@ rt_status rt_server_get_stats(rt_server* S, RtServerStats* out) {
   return RT_OK;
 }
 
+rt_status rt_server_set_batching(rt_server* S, uint32_t max_batch_jobs, uint32_t max_inflight) {
+  if (!S || max_batch_jobs == 0 || max_batch_jobs > 8192 || max_inflight == 0 || max_inflight > S->streams.size()) {
+    set_error("rt_server_set_batching: 1 <= max_batch_jobs <= 8192, 1 <= max_inflight <= streams");
+    return RT_EINVAL;
+  }
+  std::lock_guard<std::mutex> lk(S->mu);
+  S->opt.max_batch_jobs = max_batch_jobs;
+  S->opt.max_inflight = max_inflight;
+  S->cv_work.notify_all();
+  return RT_OK;
+}
+
 rt_status rt_server_autotune(rt_server* S, uint32_t scene_id, const RtRay* d_rays, uint32_t n, RtHit* d_hits) {
   if (!S) return RT_EINVAL;
   RtJob j{scene_id, n, d_rays, d_hits};

@@ -54,13 +54,32 @@ def config4(count: int = 256, tri_range=(1_000, 256_000), ray_range=(4_000, 1_00
 
 
 def config5_scene(i: int, tri_range=(64_000, 4_000_000)):
-    """Scene i of the serving workload (resident scenes and later uploads)."""
+    """Scene i of the serving workload (resident scenes and later uploads).
+
+    Stored scaled to the unit cube: n triangles with vertex offsets
+    N(0, (0.002/s)^2), s = soup_side(n) -- config 4's construction divided by s,
+    so that one batch of unit-cube rays serves every scene.  Traversal work is
+    invariant under the uniform scaling; t values scale by 1/s."""
     u = gen_uniform(5, 1_000_000 + i, 1)
     nt = int(np.rint(log_uniform(u[0], *tri_range)))
-    return gen_soup(5, i + 1, nt, soup_side(nt), 0.002)
+    return gen_soup(5, i + 1, nt, 1.0, 0.002 / soup_side(nt))
 
 
-def config5_rays(scene_tris: int, request: int, ray_range=(1_000, 2_000_000)):
-    u = gen_uniform(5, 2_000_000 + request, 1)
-    n = int(np.rint(log_uniform(u[0], *ray_range)))
-    return gen_rays(5, 3_000_000 + request, n, soup_side(scene_tris), 1e-4, float("inf"))
+def config5_requests(count: int, rate: float, n_scenes: int, upload_frac: float = 0.1,
+                     ray_range=(1_000, 2_000_000), seed_stream: int = 0):
+    """Poisson arrivals: -> list of (t_arrival, kind, scene_or_upload_index, n_rays, ray_offset)."""
+    u = gen_uniform(5, 4_000_000 + seed_stream, 5 * count)
+    t = 0.0
+    out = []
+    up = 0
+    for k in range(count):
+        t += -np.log(1.0 - u[5 * k]) / rate
+        if u[5 * k + 1] < upload_frac:
+            out.append((t, "upload", up, 0, 0))
+            up += 1
+        else:
+            n = int(np.rint(log_uniform(u[5 * k + 2], *ray_range)))
+            sid = min(int(u[5 * k + 3] * n_scenes), n_scenes - 1)
+            off = int(u[5 * k + 4] * (ray_range[1] - n + 1))
+            out.append((t, "rays", sid, n, off))
+    return out
