@@ -44,6 +44,10 @@ N_RAYS = 16_777_216
 SEED = 3
 CPU_SAMPLE = 262_144
 COUNT_SAMPLE = 65_536
+# DRAM bytes per ray of k_trace_step on the full config-3 BVH, from the ncu
+# capture summarised in profiles/k_trace_step_config3.md (2,097,152 rays,
+# dram__bytes_read.sum + dram__bytes_write.sum = 2.502 GB).
+DRAM_BYTES_PER_RAY = 2.502e9 / 2_097_152
 
 
 def parse():
@@ -62,6 +66,7 @@ def parse():
     p.add_argument("--no-sort", action="store_true", help="trace in the given ray order (no RT_TRACE_SORT)")
     p.add_argument("--no-batched", action="store_true", help="skip the config-4 batched comparison")
     p.add_argument("--no-served", action="store_true", help="skip the config-5 serving run")
+    p.add_argument("--no-render", action="store_true", help="skip the config-2 path-tracing run")
     p.add_argument("--serve-requests", type=int, default=200)
     p.add_argument("--serve-rates", type=str, default="1000,4000,8000", help="Poisson arrival rates (requests/s)")
     return p.parse_args()
@@ -229,6 +234,30 @@ def run_batched(torch, rt) -> dict:
     pool.close()
     for sc in scenes:
         sc.close()
+    return out
+
+
+def run_render(torch, rt) -> dict:
+    """Config 2: 64 displaced icospheres (subdiv 6), 1280x720, 16 samples,
+    depth 8, one rt_render call (all samples), extended shading (metal,
+    dielectric, sky colour) and reference shading."""
+    tris, mats = rt.gen_spheres_scene(2, 64, 6, 0.05)
+    w, h, spp = 1280, 720, 16
+    ubo = rt.make_ubo((0.0, 3.0, 28.0), (0.0, 0.0, 0.0), fov=40.0, depth=8, random_state=2,
+                      num_triangles=len(tris), num_materials=len(mats))
+    out = {"workload": "config 2: 64 icospheres subdiv 6 (5,242,880 triangles), radial value-noise displacement "
+                       "0.05, lambertian/metal/dielectric, 1280x720, 16 spp, depth 8",
+           "triangles": int(len(tris)), "paths": w * h * spp, "unit": "Mpaths/s"}
+    with rt.Scene(tris, materials=mats) as sc:
+        acc = torch.empty(w * h * 4, dtype=torch.float32, device="cuda")
+        for mode, name in ((rt.SHADE_EXTENDED, "extended"), (rt.SHADE_REFERENCE, "reference")):
+            def frame():
+                rt.accum_clear(acc, w, h)
+                sc.render(ubo, acc, w, h, spp, shade_mode=mode, background=(0.6, 0.7, 1.0))
+            ms = _time_events(torch, frame, warmup=1, reps=3)
+            img = acc.cpu().numpy().reshape(h, w, 4)
+            out[name] = {"value": w * h * spp / ms / 1e3, "ms_per_frame": ms,
+                         "mean_rgb": [float(img[..., k].mean() / spp) for k in range(3)]}
     return out
 
 
@@ -426,6 +455,7 @@ def run_ours(args):
     if rank != 0:
         return
     batched = None if args.no_batched else run_batched(torch, rt)
+    render = None if args.no_render else run_render(torch, rt)
     served = None if args.no_served else run_served(
         torch, rt, args.serve_requests, [float(x) for x in args.serve_rates.split(",") if x])
     peak, peak_kind = measured_peak()
@@ -442,8 +472,12 @@ def run_ours(args):
         b_ray = 32 + 8 + 32 * counts["node_boxes_per_ray"] + 48 * counts["tri_tests_per_ray"]
         avg_launch = statistics.mean(launch_ms) / 1e3
         achieved = b_ray * n / avg_launch / 1e9
+        full3 = (args.tris, n) == (N_TRIS, N_RAYS) and sort and info.node_width == 4
         roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                "traffic": None, "peak_kind": peak_kind,
+                "traffic": DRAM_BYTES_PER_RAY * n if full3 else None,
+                "traffic_note": "ncu dram bytes of a 2,097,152-ray launch on the same BVH, scaled by rays "
+                                "(profiles/k_trace_step_config3.md)" if full3 else "not captured for this shape",
+                "peak_kind": peak_kind,
                 "bytes_per_ray": b_ray, "node_boxes_per_ray": counts["node_boxes_per_ray"],
                 "tri_tests_per_ray": counts["tri_tests_per_ray"],
                 "kernel": f"k_trace_step<closest> (persistent warps, {info.node_width}-wide nodes)"
@@ -464,7 +498,7 @@ def run_ours(args):
                        "ray_order": "origin-bucketed inside the step (RT_TRACE_SORT)" if sort else "as given",
                        "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU"},
             "roofline": roof, "cpu_baseline": cpu_base, "e2e": e2e, "clocks": clk,
-            "batched": batched, "served": served,
+            "batched": batched, "served": served, "render": render,
             "gpu_launches": args.steps * (4 if sort else 1), "parity_sample": parity,
             "scene_build_s": info.build_seconds}
     print(json.dumps(line), flush=True)
