@@ -237,6 +237,29 @@ def run_batched(torch, rt) -> dict:
     return out
 
 
+def run_extras(torch, rt, scene, tris, d_rays, n: int) -> dict:
+    """Config 3 any-hit, the BVH build on host vs device, config 1 closest-hit."""
+    d_hits = torch.empty(n * 8, dtype=torch.uint8, device="cuda")
+    ms_any = _time_events(torch, lambda: scene.trace(d_rays, d_hits, any_hit=True, sort=True), warmup=2, reps=10)
+    t0 = time.perf_counter()
+    rt.build_bvh(tris)
+    host_s = time.perf_counter() - t0
+    d_t = torch.from_numpy(tris.view(np.uint8)).cuda()
+    d_n = torch.empty((2 * len(tris) - 1) * 40, dtype=torch.uint8, device="cuda")
+    ms_dev = _time_events(torch, lambda: rt.build_bvh_device(d_t, len(tris), None, 0, d_n), warmup=1, reps=5)
+    c1_tris, _, c1_rays = rt.gen_config1()
+    out = {"config3_any_hit": {"value": n / ms_any / 1e6, "unit": UNIT, "ms": ms_any},
+           "bvh_build_config3": {"host_s": host_s, "host_threads": os.cpu_count(), "device_ms": ms_dev,
+                                 "note": "2N-1 reference-layout nodes, identical bytes from both builders"}}
+    with rt.Scene(c1_tris, bvh_mode=rt.BVH_REFERENCE) as s1:
+        r1 = torch.from_numpy(c1_rays.view(np.uint8)).cuda()
+        h1 = torch.empty(len(c1_rays) * 8, dtype=torch.uint8, device="cuda")
+        ms1 = _time_events(torch, lambda: s1.trace(r1, h1), warmup=2, reps=20)
+    out["config1_closest_hit"] = {"value": len(c1_rays) / ms1 / 1e6, "unit": UNIT, "ms": ms1,
+                                  "bvh": "reference leaf order (ConstructHLBVH.comp:152-169)"}
+    return out
+
+
 def run_render(torch, rt) -> dict:
     """Config 2: 64 displaced icospheres (subdiv 6), 1280x720, 16 samples,
     depth 8, one rt_render call (all samples), extended shading (metal,
@@ -273,7 +296,7 @@ def run_served(torch, rt, n_requests: int, rates: list[float]) -> dict:
     ray_pool_t = torch.from_numpy(rt.gen_rays(5, 0, 2_000_000, 1.0, 1e-4, float("inf")).view(np.uint8)).pin_memory()
     ray_pool = ray_pool_t.numpy().view(rt.RAY_DTYPE)
     srv = rt.Server(budget_bytes=150 << 30, max_inflight=3, max_batch_rays=1 << 23)
-    sids = [srv.wait(srv.upload(t), 600.0).scene_id for t in resident]
+    sids = [srv.wait(srv.upload(t, build_on_device=True), 600.0).scene_id for t in resident]
     setup_s = time.perf_counter() - t0
     res_tris = int(sum(len(t) for t in resident))
     runs = []
@@ -298,7 +321,7 @@ def run_served(torch, rt, n_requests: int, rates: list[float]) -> dict:
                 if delay > 0:
                     time.sleep(delay)
                 if kind == "upload":
-                    ids.append(srv.upload(uploads[idx]))
+                    ids.append(srv.upload(uploads[idx], build_on_device=True))
                 else:
                     ids.append(srv.submit(sids[idx], ray_pool[off:off + n], hits[hoff:hoff + n]))
                     hoff += n
@@ -329,7 +352,7 @@ def run_served(torch, rt, n_requests: int, rates: list[float]) -> dict:
     srv.close()
     return {"workload": "config 5: 64 resident soups (counts log-uniform in [64K, 4M]), Poisson arrivals, "
                         "90% closest-hit queries of log-uniform [1K, 2M] rays from pinned host memory, "
-                        "10% new-scene uploads; HBM budget 150 GB",
+                        "10% new-scene uploads (BVH built on the GPU); HBM budget 150 GB",
             "resident_triangles": res_tris, "setup_s": setup_s, "runs": runs,
             "batches_total": int(st.batches), "evictions": int(st.evictions),
             "latency": "submit of the host request to its hits back in host memory",
@@ -454,6 +477,7 @@ def run_ours(args):
 
     if rank != 0:
         return
+    extras = run_extras(torch, rt, scene, tris, d_rays, n) if (args.tris, args.rays) == (N_TRIS, N_RAYS) else None
     batched = None if args.no_batched else run_batched(torch, rt)
     render = None if args.no_render else run_render(torch, rt)
     served = None if args.no_served else run_served(
@@ -498,7 +522,7 @@ def run_ours(args):
                        "ray_order": "origin-bucketed inside the step (RT_TRACE_SORT)" if sort else "as given",
                        "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU"},
             "roofline": roof, "cpu_baseline": cpu_base, "e2e": e2e, "clocks": clk,
-            "batched": batched, "served": served, "render": render,
+            "batched": batched, "served": served, "render": render, "extras": extras,
             "gpu_launches": args.steps * (4 if sort else 1), "parity_sample": parity,
             "scene_build_s": info.build_seconds}
     print(json.dumps(line), flush=True)

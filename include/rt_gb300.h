@@ -166,7 +166,10 @@ typedef struct RtSceneDesc {
   uint32_t bvh_mode;              /* RT_BVH_SORTED | RT_BVH_REFERENCE */
   uint32_t leaf_size;             /* max triangles per device leaf after collapsing; 0 = default (1) */
   uint32_t node_width;            /* device BVH width: 2 (binary) or 4 (quantised); 0 = default (4) */
+  uint32_t build_flags;           /* RT_BUILD_ON_DEVICE: build the node array with rt_build_bvh_device */
 } RtSceneDesc;
+
+#define RT_BUILD_ON_DEVICE 1u
 
 typedef struct RtSceneInfo {
   uint32_t num_triangles;
@@ -205,6 +208,15 @@ rt_status rt_build_bvh(const RtTriangle64* triangles, uint32_t num_triangles,
                        const RtSphere32* spheres, uint32_t num_spheres,
                        const RtModel64* models, uint32_t num_models,
                        uint32_t bvh_mode, RtBVHNode40* out_nodes);
+
+/* The same six S1 passes on the GPU (device in, device out), bit-identical to
+ * rt_build_bvh: centroid box, 30-bit Morton codes, stable radix sort of
+ * (code, index) in four 8-bit passes, Karras hierarchy, bottom-up boxes.
+ * d_nodes holds 2*(num_triangles+num_spheres)-1 records.  Stream-ordered;
+ * its scratch comes from the stream-ordered allocator (cudaMallocAsync). */
+rt_status rt_build_bvh_device(const RtTriangle64* d_triangles, uint32_t num_triangles,
+                              const RtSphere32* d_spheres, uint32_t num_spheres, uint32_t bvh_mode,
+                              RtBVHNode40* d_nodes, void* stream);
 
 /* ------------------------------------------------------------------ trace */
 enum {

@@ -72,7 +72,9 @@ class _SceneDesc(C.Structure):
                 ("num_spheres", C.c_uint32), ("materials", C.c_void_p), ("num_materials", C.c_uint32),
                 ("models", C.c_void_p), ("num_models", C.c_uint32), ("nodes", C.c_void_p),
                 ("num_nodes", C.c_uint32), ("bvh_mode", C.c_uint32), ("leaf_size", C.c_uint32),
-                ("node_width", C.c_uint32)]
+                ("node_width", C.c_uint32), ("build_flags", C.c_uint32)]
+
+BUILD_ON_DEVICE = 1
 
 
 class SceneInfo(C.Structure):
@@ -133,6 +135,7 @@ SIGNATURES = {
     "rt_scene_get_info": (_I, [_P, C.POINTER(SceneInfo)]),
     "rt_scene_get_nodes": (_I, [_P, _P, _U32]),
     "rt_build_bvh": (_I, [_P, _U32, _P, _U32, _P, _U32, _U32, _P]),
+    "rt_build_bvh_device": (_I, [_P, _U32, _P, _U32, _U32, _P, _P]),
     "rt_trace": (_I, [_P, _P, _U32, _P, _U32, _P]),
     "rt_trace_host": (_I, [_P, _P, _U32, _P, _U32, _P]),
     "rt_trace_count": (_I, [_P, _P, _U32, _P, _U32, _P, C.POINTER(_U64)]),
@@ -232,7 +235,7 @@ class Scene:
     """
 
     def __init__(self, triangles, spheres=None, materials=None, models=None, nodes=None,
-                 bvh_mode: int = BVH_SORTED, leaf_size: int = 0, node_width: int = 0):
+                 bvh_mode: int = BVH_SORTED, leaf_size: int = 0, node_width: int = 0, build_on_device: bool = False):
         L = lib()
         tri = np.ascontiguousarray(triangles, dtype=TRIANGLE_DTYPE) if triangles is not None else np.zeros(0, TRIANGLE_DTYPE)
         sph = np.ascontiguousarray(spheres, dtype=SPHERE_DTYPE) if spheres is not None else np.zeros(0, SPHERE_DTYPE)
@@ -241,7 +244,7 @@ class Scene:
         nod = np.ascontiguousarray(nodes, dtype=NODE_DTYPE) if nodes is not None else None
         d = _SceneDesc(_ptr(tri), len(tri), _ptr(sph), len(sph), _ptr(mat), len(mat),
                        _ptr(mod), 0 if mod is None else len(mod), _ptr(nod), 0 if nod is None else len(nod),
-                       bvh_mode, leaf_size, node_width)
+                       bvh_mode, leaf_size, node_width, BUILD_ON_DEVICE if build_on_device else 0)
         h = C.c_void_p()
         _check(L.rt_scene_create_ex(C.byref(d), C.byref(h)), "rt_scene_create_ex")
         self._h = h
@@ -320,12 +323,12 @@ class Scene:
         self.close()
 
 
-def _desc(triangles, models=None, nodes=None, bvh_mode=BVH_SORTED, leaf_size=0, node_width=0):
+def _desc(triangles, models=None, nodes=None, bvh_mode=BVH_SORTED, leaf_size=0, node_width=0, build_flags=0):
     tri = np.ascontiguousarray(triangles, dtype=TRIANGLE_DTYPE)
     mod = np.ascontiguousarray(models, dtype=MODEL_DTYPE) if models is not None else None
     nod = np.ascontiguousarray(nodes, dtype=NODE_DTYPE) if nodes is not None else None
     d = _SceneDesc(_ptr(tri), len(tri), None, 0, None, 0, _ptr(mod), 0 if mod is None else len(mod),
-                   _ptr(nod), 0 if nod is None else len(nod), bvh_mode, leaf_size, node_width)
+                   _ptr(nod), 0 if nod is None else len(nod), bvh_mode, leaf_size, node_width, build_flags)
     return d, (tri, mod, nod)
 
 
@@ -348,8 +351,9 @@ class Pool:
             raise ValueError("pool destroyed")
         return self._h.value
 
-    def add_scene(self, triangles, models=None, nodes=None, bvh_mode: int = BVH_SORTED, leaf_size: int = 0) -> int:
-        d, keep = _desc(triangles, models, nodes, bvh_mode, leaf_size, 4)
+    def add_scene(self, triangles, models=None, nodes=None, bvh_mode: int = BVH_SORTED, leaf_size: int = 0,
+                  build_on_device: bool = False) -> int:
+        d, keep = _desc(triangles, models, nodes, bvh_mode, leaf_size, 4, BUILD_ON_DEVICE if build_on_device else 0)
         sid = C.c_uint32()
         _check(lib().rt_pool_add_scene(self.handle, C.byref(d), C.byref(sid)), "rt_pool_add_scene")
         return sid.value
@@ -423,8 +427,8 @@ class Server:
             raise ValueError("server destroyed")
         return self._h.value
 
-    def upload(self, triangles, models=None, bvh_mode: int = BVH_SORTED) -> int:
-        d, keep = _desc(triangles, models, None, bvh_mode, 0, 4)
+    def upload(self, triangles, models=None, bvh_mode: int = BVH_SORTED, build_on_device: bool = False) -> int:
+        d, keep = _desc(triangles, models, None, bvh_mode, 0, 4, BUILD_ON_DEVICE if build_on_device else 0)
         rid = C.c_uint64()
         _check(lib().rt_server_upload(self.handle, C.byref(d), C.byref(rid)), "rt_server_upload")
         self._keep[rid.value] = (d, keep)
@@ -505,6 +509,14 @@ def build_bvh(triangles, spheres=None, models=None, bvh_mode: int = BVH_SORTED) 
     _check(lib().rt_build_bvh(_ptr(tri), len(tri), _ptr(sph), len(sph), _ptr(mod), 0 if mod is None else len(mod),
                               bvh_mode, _ptr(out)), "rt_build_bvh")
     return out
+
+
+def build_bvh_device(d_triangles, num_triangles: int, d_spheres=None, num_spheres: int = 0, d_nodes=None,
+                     bvh_mode: int = BVH_SORTED, stream=None):
+    """rt_build_bvh_device on device buffers (torch tensors); returns d_nodes."""
+    _check(lib().rt_build_bvh_device(_ptr(d_triangles), num_triangles, _ptr(d_spheres), num_spheres, bvh_mode,
+                                     _ptr(d_nodes), _stream_handle(stream)), "rt_build_bvh_device")
+    return d_nodes
 
 
 def accum_clear(accum, width: int, height: int, stream=None) -> None:

@@ -73,6 +73,31 @@ static rt_status workspace(cudaStream_t st, Workspace** out) {
   return RT_OK;
 }
 
+// Builds the node array on the GPU from host primitives and copies it back.
+rt_status device_build_to_host(const RtTriangle64* tris, uint32_t nt, const RtSphere32* sph, uint32_t ns,
+                               uint32_t mode, std::vector<RtBVHNode40>& out) {
+  const uint64_t N = (uint64_t)nt + ns;
+  RtTriangle64* d_t = nullptr;
+  RtSphere32* d_s = nullptr;
+  RtBVHNode40* d_n = nullptr;
+  cudaError_t e = cudaMalloc(&d_t, sizeof(RtTriangle64) * (nt ? nt : 1));
+  if (e == cudaSuccess) e = cudaMalloc(&d_s, sizeof(RtSphere32) * (ns ? ns : 1));
+  if (e == cudaSuccess) e = cudaMalloc(&d_n, sizeof(RtBVHNode40) * (2 * N - 1));
+  if (e == cudaSuccess && nt) e = cudaMemcpy(d_t, tris, sizeof(RtTriangle64) * nt, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess && ns) e = cudaMemcpy(d_s, sph, sizeof(RtSphere32) * ns, cudaMemcpyHostToDevice);
+  rt_status st = RT_OK;
+  if (e == cudaSuccess) st = rt_build_bvh_device(d_t, nt, d_s, ns, mode, d_n, nullptr);
+  if (e == cudaSuccess && st == RT_OK) {
+    out.resize(2 * N - 1);
+    e = cudaMemcpy(out.data(), d_n, sizeof(RtBVHNode40) * (2 * N - 1), cudaMemcpyDeviceToHost);
+  }
+  cudaFree(d_t);
+  cudaFree(d_s);
+  cudaFree(d_n);
+  if (st != RT_OK) return st;
+  return e == cudaSuccess ? RT_OK : cuda_fail(e, "device BVH build");
+}
+
 // Reorders the batch when RT_TRACE_SORT is set; *order = nullptr otherwise.
 static rt_status maybe_reorder(Workspace* w, const DeviceScene& d, const RtRay* rays, uint32_t n, uint32_t flags,
                                cudaStream_t st, uint32_t** order) {
@@ -177,6 +202,9 @@ rt_status rt_scene_create_ex(const RtSceneDesc* desc, rt_scene** out_scene) {
   }
   if (desc->nodes) {
     sc->nodes40.assign(desc->nodes, desc->nodes + (N ? 2 * N - 1 : 0));
+  } else if ((desc->build_flags & RT_BUILD_ON_DEVICE) && N) {
+    rt_status bs = device_build_to_host(wt.data(), nt, ws.data(), ns, desc->bvh_mode, sc->nodes40);
+    if (bs != RT_OK) return bs;
   } else {
     build_bvh(wt.data(), nt, ws.data(), ns, desc->bvh_mode, sc->nodes40);
   }

@@ -26,6 +26,8 @@
 namespace rtgb {
 
 void set_error(const std::string& msg);
+rt_status device_build_to_host(const RtTriangle64* tris, uint32_t nt, const RtSphere32* sph, uint32_t ns,
+                               uint32_t mode, std::vector<RtBVHNode40>& out);
 
 namespace {
 
@@ -487,10 +489,14 @@ rt_status rt_pool_add_scene(rt_pool* P, const RtSceneDesc* desc, uint32_t* out_i
     return RT_EINVAL;
   }
   std::vector<RtBVHNode40> nodes;
-  if (desc->nodes)
+  if (desc->nodes) {
     nodes.assign(desc->nodes, desc->nodes + (nt ? 2 * (size_t)nt - 1 : 0));
-  else
+  } else if ((desc->build_flags & RT_BUILD_ON_DEVICE) && nt) {
+    rt_status bs = device_build_to_host(wt.data(), nt, nullptr, 0, desc->bvh_mode, nodes);
+    if (bs != RT_OK) return bs;
+  } else {
     build_bvh(wt.data(), nt, nullptr, 0, desc->bvh_mode, nodes);
+  }
   HostDeviceBVH hb;
   if (!convert_bvh(nodes.data(), (uint32_t)nodes.size(), wt.data(), nt, nullptr, 0, nullptr, 0, desc->leaf_size, 4, hb,
                    msg)) {

@@ -155,5 +155,9 @@ cudaError_t launch_render(const DeviceScene& s, const float cam[12], uint32_t de
 cudaError_t launch_accum_clear(float* accum, uint32_t w, uint32_t h, void* stream);
 cudaError_t launch_resolve(const float* accum, uint32_t w, uint32_t h, uint32_t spp, float* out, void* stream);
 int device_sm_count();
+// GPU LBVH build (gpu_build.cu)
+size_t device_build_scratch_bytes(uint32_t n);
+cudaError_t launch_device_build(const RtTriangle64* tris, uint32_t nt, const RtSphere32* sph, uint32_t ns,
+                                uint32_t mode, RtBVHNode40* nodes, void* scratch, cudaStream_t st);
 
 }  // namespace rtgb
