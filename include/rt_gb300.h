@@ -412,6 +412,20 @@ rt_status rt_accum_clear(float* d_accum, uint32_t width, uint32_t height, void* 
 rt_status rt_resolve(const float* d_accum, uint32_t width, uint32_t height, uint32_t spp,
                      float* d_out, void* stream);
 
+/* ------------------------------------------------------- scene ingestion */
+/* Wavefront OBJ -> triangles, as the reference's loadModel (RTModel.cpp:47-108,
+ * tinyobjloader): face vertex positions, polygons fanned from their first
+ * vertex, file order.  Call with out = NULL to get the count. */
+rt_status rt_obj_load(const char* path, uint32_t material, RtTriangle64* out, uint64_t capacity, uint64_t* count);
+/* TransformComponent::mat4 (TransformComponent.cpp:9-45): translate * Ry * Rx * Rz * scale,
+ * Tait-Bryan Y-X-Z angles in radians, column-major. */
+rt_status rt_model_matrix(const float translation[3], const float rotation[3], const float scale[3],
+                          RtModel64* out);
+/* Headless stand-ins for the present pass: a W*H RGBA float image (e.g. from
+ * rt_resolve, copied to the host) to binary PPM (8-bit, top row first) or PFM. */
+rt_status rt_write_ppm(const char* path, const float* h_rgba, uint32_t width, uint32_t height);
+rt_status rt_write_pfm(const char* path, const float* h_rgba, uint32_t width, uint32_t height);
+
 /* --------------------------------------------------------------- utility */
 const char* rt_last_error_string(void);
 uint32_t rt_abi_version(void);

@@ -163,6 +163,10 @@ SIGNATURES = {
     "rt_server_get_stats": (_I, [_P, C.POINTER(ServerStats)]),
     "rt_server_autotune": (_I, [_P, _U32, _P, _U32, _P]),
     "rt_server_set_batching": (_I, [_P, _U32, _U32]),
+    "rt_obj_load": (_I, [C.c_char_p, _U32, _P, _U64, C.POINTER(_U64)]),
+    "rt_model_matrix": (_I, [_P, _P, _P, _P]),
+    "rt_write_ppm": (_I, [C.c_char_p, _P, _U32, _U32]),
+    "rt_write_pfm": (_I, [C.c_char_p, _P, _U32, _U32]),
     "rt_gen_uniform": (_I, [_U64, _U64, _U64, _P]),
     "rt_gen_icosphere": (_I, [_U32, _P, _F, _U32, _P, _U64, C.POINTER(_U64)]),
     "rt_gen_config1": (_I, [_P, C.POINTER(RaytracingUBO), _P]),
@@ -517,6 +521,32 @@ def build_bvh_device(d_triangles, num_triangles: int, d_spheres=None, num_sphere
     _check(lib().rt_build_bvh_device(_ptr(d_triangles), num_triangles, _ptr(d_spheres), num_spheres, bvh_mode,
                                      _ptr(d_nodes), _stream_handle(stream)), "rt_build_bvh_device")
     return d_nodes
+
+
+def load_obj(path, material: int = 0) -> np.ndarray:
+    """Triangles of an OBJ file (positions, fan-triangulated faces, file order)."""
+    cnt = C.c_uint64()
+    _check(lib().rt_obj_load(str(path).encode(), material, None, 0, C.byref(cnt)), "rt_obj_load")
+    out = np.zeros(cnt.value, TRIANGLE_DTYPE)
+    _check(lib().rt_obj_load(str(path).encode(), material, _ptr(out), cnt.value, C.byref(cnt)), "rt_obj_load")
+    return out
+
+
+def model_matrix(translation=(0.0, 0.0, 0.0), rotation=(0.0, 0.0, 0.0), scale=(1.0, 1.0, 1.0)) -> np.ndarray:
+    """TransformComponent::mat4 as a MODEL_DTYPE record (column-major)."""
+    t = np.asarray(translation, np.float32)
+    r = np.asarray(rotation, np.float32)
+    s = np.asarray(scale, np.float32)
+    out = np.zeros(1, MODEL_DTYPE)
+    _check(lib().rt_model_matrix(_ptr(t), _ptr(r), _ptr(s), _ptr(out)), "rt_model_matrix")
+    return out
+
+
+def write_image(path, rgba: np.ndarray, width: int, height: int) -> None:
+    """RGBA float image (host) to .ppm (8-bit) or .pfm (float)."""
+    rgba = np.ascontiguousarray(rgba, dtype=np.float32)
+    fn = lib().rt_write_pfm if str(path).endswith(".pfm") else lib().rt_write_ppm
+    _check(fn(str(path).encode(), _ptr(rgba), width, height), "rt_write_image")
 
 
 def accum_clear(accum, width: int, height: int, stream=None) -> None:
