@@ -42,7 +42,7 @@ UNIT = "Grays/s"
 N_TRIS = 4_194_304
 N_RAYS = 16_777_216
 SEED = 3
-CPU_SAMPLE = 262_144
+CPU_SAMPLE = 2_097_152
 COUNT_SAMPLE = 65_536
 # DRAM bytes per ray of k_trace_step on the full config-3 BVH, from the ncu
 # capture summarised in profiles/k_trace_step_config3.md (2,097,152 rays,

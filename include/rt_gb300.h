@@ -427,6 +427,11 @@ rt_status rt_write_ppm(const char* path, const float* h_rgba, uint32_t width, ui
 rt_status rt_write_pfm(const char* path, const float* h_rgba, uint32_t width, uint32_t height);
 
 /* --------------------------------------------------------------- utility */
+/* Device memory for callers without CUDA headers (the C++ mirror uses these). */
+rt_status rt_device_alloc(size_t bytes, void** d_out);
+rt_status rt_device_free(void* d_ptr);
+/* Stream-ordered copies; host memory pinned or pageable. */
+rt_status rt_copy(void* dst, const void* src, size_t bytes, void* stream);
 const char* rt_last_error_string(void);
 uint32_t rt_abi_version(void);
 /* Waits for the stream with a deadline; RT_ETIMEOUT when it runs out. */

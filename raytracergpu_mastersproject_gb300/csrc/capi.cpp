@@ -126,6 +126,29 @@ using namespace rtgb;
 extern "C" {
 
 const char* rt_last_error_string(void) { return g_error.c_str(); }
+
+rt_status rt_device_alloc(size_t bytes, void** d_out) {
+  if (!d_out) return RT_EINVAL;
+  *d_out = nullptr;
+  cudaError_t e = cudaMalloc(d_out, bytes ? bytes : 1);
+  if (e != cudaSuccess) {
+    set_error(std::string("rt_device_alloc: ") + cudaGetErrorString(e));
+    return RT_ENOMEM;
+  }
+  return RT_OK;
+}
+
+rt_status rt_device_free(void* d_ptr) {
+  cudaError_t e = cudaFree(d_ptr);
+  return e == cudaSuccess ? RT_OK : cuda_fail(e, "rt_device_free");
+}
+
+rt_status rt_copy(void* dst, const void* src, size_t bytes, void* stream) {
+  if ((!dst || !src) && bytes) return RT_EINVAL;
+  if (!bytes) return RT_OK;
+  cudaError_t e = cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDefault, reinterpret_cast<cudaStream_t>(stream));
+  return e == cudaSuccess ? RT_OK : cuda_fail(e, "rt_copy");
+}
 uint32_t rt_abi_version(void) { return RT_ABI_VERSION; }
 
 rt_status rt_stream_wait(void* stream, double timeout_seconds) {
