@@ -5,6 +5,7 @@
 // nodes.  Per-stream work counters (the persistent kernels' ray/pixel
 // queues) live in a small per-(device, stream) workspace created on first use.
 #include <chrono>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <memory>
@@ -46,6 +47,7 @@ struct Workspace {
   void* sort = nullptr;
   size_t sort_bytes = 0;
   cudaStream_t copy_in = nullptr, copy_out = nullptr;
+  cudaStream_t trace2 = nullptr;  // second trace stream of rt_trace_host
   cudaEvent_t ev[8] = {};
 };
 static std::mutex g_ws_mu;
@@ -98,24 +100,32 @@ rt_status device_build_to_host(const RtTriangle64* tris, uint32_t nt, const RtSp
   return e == cudaSuccess ? RT_OK : cuda_fail(e, "device BVH build");
 }
 
+static rt_status ensure_sort_scratch(Workspace* w, size_t need) {
+  if (w->sort_bytes >= need) return RT_OK;
+  if (w->sort) cudaFree(w->sort);
+  w->sort = nullptr;
+  w->sort_bytes = 0;
+  cudaError_t e = cudaMalloc(&w->sort, need);
+  if (e != cudaSuccess) {
+    set_error(std::string("reorder scratch: cudaMalloc: ") + cudaGetErrorString(e));
+    return RT_ENOMEM;
+  }
+  w->sort_bytes = need;
+  return RT_OK;
+}
+
+static size_t sort_slot_bytes(uint32_t n) { return (reorder_scratch_bytes(n) + 255) & ~(size_t)255; }
+
 // Reorders the batch when RT_TRACE_SORT is set; *order = nullptr otherwise.
+// The scratch starts `offset` bytes into the workspace's sort buffer, so that
+// batches in flight on two streams use disjoint regions.
 static rt_status maybe_reorder(Workspace* w, const DeviceScene& d, const RtRay* rays, uint32_t n, uint32_t flags,
-                               cudaStream_t st, uint32_t** order) {
+                               cudaStream_t st, uint32_t** order, size_t offset = 0) {
   *order = nullptr;
   if (!(flags & RT_TRACE_SORT) || d.root == kSentinel) return RT_OK;
-  const size_t need = reorder_scratch_bytes(n);
-  if (w->sort_bytes < need) {
-    if (w->sort) cudaFree(w->sort);
-    w->sort = nullptr;
-    w->sort_bytes = 0;
-    cudaError_t e = cudaMalloc(&w->sort, need);
-    if (e != cudaSuccess) {
-      set_error(std::string("reorder scratch: cudaMalloc: ") + cudaGetErrorString(e));
-      return RT_ENOMEM;
-    }
-    w->sort_bytes = need;
-  }
-  cudaError_t e = launch_reorder(d, rays, n, w->sort, order, st);
+  rt_status s = ensure_sort_scratch(w, offset + reorder_scratch_bytes(n));
+  if (s != RT_OK) return s;
+  cudaError_t e = launch_reorder(d, rays, n, static_cast<char*>(w->sort) + offset, order, st);
   return e == cudaSuccess ? RT_OK : cuda_fail(e, "reorder");
 }
 
@@ -427,10 +437,25 @@ rt_status rt_trace_host(rt_scene* scene, const RtRay* h_rays, uint32_t n, RtHit*
   Workspace* w = nullptr;
   rt_status s = workspace(st, &w);
   if (s != RT_OK) return s;
-  // Two buffers of up to `chunk` rays; copy-in, trace and copy-out run on three
-  // streams so chunk i+1 uploads while chunk i traces and chunk i-1 downloads.
-  const uint32_t chunk = std::min<uint32_t>(n, 1u << 21);
-  const uint32_t nchunks = (n + chunk - 1) / chunk;
+  // Chunks alternate between two buffers and two trace streams (the caller's
+  // and trace2), each with its own counters and reorder scratch; copy-in and
+  // copy-out run on streams of their own, so chunk i+1 uploads and chunk i-1
+  // downloads while chunk i traces, and chunk i+1's blocks take the SMs that
+  // chunk i's last rays leave idle.  Every launch still ends with a drain of
+  // its in-flight rays at falling SIMT efficiency, so chunks are few and
+  // large: the first is small (its upload is not overlapped) and each next
+  // one 4x larger, up to the buffer size.
+  static const uint32_t kMaxChunk = [] {
+    const char* e = std::getenv("RT_HOST_CHUNK_RAYS");
+    const long v = e ? std::atol(e) : 0;
+    return v >= 4096 && v <= (1l << 30) ? (uint32_t)v : (1u << 23);
+  }();
+  static const uint32_t kFirstChunk = [] {
+    const char* e = std::getenv("RT_HOST_FIRST_CHUNK_RAYS");
+    const long v = e ? std::atol(e) : 0;
+    return v >= 4096 && v <= (1l << 30) ? (uint32_t)v : (1u << 19);
+  }();
+  const uint32_t chunk = std::min<uint32_t>(n, kMaxChunk);  // buffer capacity
   const size_t per = (size_t)chunk * (sizeof(RtRay) + sizeof(RtHit));
   const size_t need = 2 * per;
   cudaError_t e;
@@ -445,9 +470,12 @@ rt_status rt_trace_host(rt_scene* scene, const RtRay* h_rays, uint32_t n, RtHit*
     }
     w->stage_bytes = need;
   }
+  const size_t slot = sort_slot_bytes(chunk);
+  if ((flags & RT_TRACE_SORT) && (s = ensure_sort_scratch(w, 2 * slot)) != RT_OK) return s;
   if (!w->copy_in) {
     if ((e = cudaStreamCreateWithFlags(&w->copy_in, cudaStreamNonBlocking)) != cudaSuccess) return cuda_fail(e, "stream");
     if ((e = cudaStreamCreateWithFlags(&w->copy_out, cudaStreamNonBlocking)) != cudaSuccess) return cuda_fail(e, "stream");
+    if ((e = cudaStreamCreateWithFlags(&w->trace2, cudaStreamNonBlocking)) != cudaSuccess) return cuda_fail(e, "stream");
     for (auto& ev : w->ev)
       if ((e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming)) != cudaSuccess) return cuda_fail(e, "event");
   }
@@ -455,35 +483,40 @@ rt_status rt_trace_host(rt_scene* scene, const RtRay* h_rays, uint32_t n, RtHit*
   RtRay* drays[2] = {reinterpret_cast<RtRay*>(base), reinterpret_cast<RtRay*>(base + per)};
   RtHit* dhits[2] = {reinterpret_cast<RtHit*>(base + (size_t)chunk * sizeof(RtRay)),
                      reinterpret_cast<RtHit*>(base + per + (size_t)chunk * sizeof(RtRay))};
+  cudaStream_t tst[2] = {st, w->trace2};
+  uint32_t* counters[2] = {w->counters, w->counters + 4};
   cudaEvent_t* in_done = &w->ev[0];
   cudaEvent_t* trace_done = &w->ev[2];
   cudaEvent_t* out_done = &w->ev[4];
-  // the caller's earlier work on `stream` comes first
+  // the caller's earlier work on `stream` comes first (trace2 follows it
+  // through copy_in's events)
   if ((e = cudaEventRecord(w->ev[6], st)) != cudaSuccess) return cuda_fail(e, "event");
   if ((e = cudaStreamWaitEvent(w->copy_in, w->ev[6], 0)) != cudaSuccess) return cuda_fail(e, "wait");
-  for (uint32_t c = 0; c < nchunks; ++c) {
+  uint32_t size = std::min(chunk, kFirstChunk);
+  for (uint32_t c = 0, off = 0, cnt = 0; off < n; ++c, off += cnt, size = (uint32_t)std::min<uint64_t>(4ull * size, chunk)) {
     const uint32_t b = c & 1u;
-    const uint32_t off = c * chunk;
-    const uint32_t cnt = std::min(chunk, n - off);
+    cnt = std::min(size, n - off);
+    // buffers b are free once chunk c-2 has been downloaded
     if (c >= 2 && (e = cudaStreamWaitEvent(w->copy_in, out_done[b], 0)) != cudaSuccess) return cuda_fail(e, "wait");
     if ((e = cudaMemcpyAsync(drays[b], h_rays + off, (size_t)cnt * sizeof(RtRay), cudaMemcpyHostToDevice,
                              w->copy_in)) != cudaSuccess)
       return cuda_fail(e, "rt_trace_host: H2D");
     if ((e = cudaEventRecord(in_done[b], w->copy_in)) != cudaSuccess) return cuda_fail(e, "event");
-    if ((e = cudaStreamWaitEvent(st, in_done[b], 0)) != cudaSuccess) return cuda_fail(e, "wait");
+    if ((e = cudaStreamWaitEvent(tst[b], in_done[b], 0)) != cudaSuccess) return cuda_fail(e, "wait");
     uint32_t* order = nullptr;
-    if ((s = maybe_reorder(w, scene->d, drays[b], cnt, flags, st, &order)) != RT_OK) return s;
-    if ((e = cudaMemsetAsync(w->counters, 0, 2 * sizeof(uint32_t), st)) != cudaSuccess) return cuda_fail(e, "memset");
-    if ((e = launch_trace(scene->d, drays[b], cnt, dhits[b], flags, w->counters, stream, order)) != cudaSuccess)
+    if ((s = maybe_reorder(w, scene->d, drays[b], cnt, flags, tst[b], &order, b * slot)) != RT_OK) return s;
+    if ((e = cudaMemsetAsync(counters[b], 0, 2 * sizeof(uint32_t), tst[b])) != cudaSuccess) return cuda_fail(e, "memset");
+    if ((e = launch_trace(scene->d, drays[b], cnt, dhits[b], flags, counters[b], tst[b], order)) != cudaSuccess)
       return cuda_fail(e, "rt_trace_host: launch");
-    if ((e = cudaEventRecord(trace_done[b], st)) != cudaSuccess) return cuda_fail(e, "event");
+    if ((e = cudaEventRecord(trace_done[b], tst[b])) != cudaSuccess) return cuda_fail(e, "event");
     if ((e = cudaStreamWaitEvent(w->copy_out, trace_done[b], 0)) != cudaSuccess) return cuda_fail(e, "wait");
     if ((e = cudaMemcpyAsync(h_hits + off, dhits[b], (size_t)cnt * sizeof(RtHit), cudaMemcpyDeviceToHost,
                              w->copy_out)) != cudaSuccess)
       return cuda_fail(e, "rt_trace_host: D2H");
     if ((e = cudaEventRecord(out_done[b], w->copy_out)) != cudaSuccess) return cuda_fail(e, "event");
   }
-  // the caller's stream continues after the last download
+  // the caller's stream continues after the last download (every chunk's
+  // download waited for its trace, so trace2 is drained too)
   if ((e = cudaEventRecord(w->ev[7], w->copy_out)) != cudaSuccess) return cuda_fail(e, "event");
   if ((e = cudaStreamWaitEvent(st, w->ev[7], 0)) != cudaSuccess) return cuda_fail(e, "wait");
   if ((e = cudaStreamSynchronize(w->copy_out)) != cudaSuccess) return cuda_fail(e, "rt_trace_host: sync");

@@ -116,8 +116,14 @@ def test_trace_host_matches_device(rt, cuda):
         b = sc.trace_host(rays)
         pinned = cuda.from_numpy(rays.view(np.uint8)).pin_memory()
         c = sc.trace_host(pinned.numpy().view(rt.RAY_DTYPE))
+        # 5 M rays: chunks of 512 Ki, 2 Mi and the rest, on both buffers and both trace streams
+        d = sc.trace_host(pinned.numpy().view(rt.RAY_DTYPE), sort=True)
+        e = sc.trace_host(pinned.numpy().view(rt.RAY_DTYPE), any_hit=True)
+        f = dev_trace(rt, cuda, sc, rays, any_hit=True)
     assert np.array_equal(a.view(np.uint64), b.view(np.uint64))
     assert np.array_equal(a.view(np.uint64), c.view(np.uint64))
+    assert np.array_equal(a.view(np.uint64), d.view(np.uint64))
+    assert np.array_equal(e.view(np.uint64), f.view(np.uint64))
 
 
 def test_caller_supplied_nodes(rt, orc, cuda):
