@@ -138,3 +138,38 @@ def test_golden_accumulator_on_gpu(rt, cuda):
     with rt.Scene(tris, materials=mats) as sc:
         img = gpu_render(rt, cuda, sc, ubo, w, h, spp)
     assert rmse(img, g["accum"]) <= 1e-3
+
+
+@pytest.mark.parametrize("mode", ["reference", "extended"])
+def test_step_render_matches_per_pixel_render(rt, cuda, mode):
+    """4-wide trees render with the per-lane step kernel, binary trees with
+    one thread per pixel and whole traversals.  Hits do not depend on the
+    traversal, and each pixel's samples are summed in order by both, so the
+    accumulators are bit-identical."""
+    tris, mats = rt.gen_spheres_scene(2, 64, 3, 0.05)
+    ubo = rt.make_ubo((0.0, 3.0, 28.0), (0.0, 0.0, 0.0), fov=40.0, depth=8, random_state=2,
+                      num_triangles=len(tris), num_materials=len(mats))
+    w, h, spp = 160, 90, 4
+    kw = {"shade_mode": rt.SHADE_EXTENDED, "background": (0.6, 0.7, 1.0)} if mode == "extended" else {}
+    with rt.Scene(tris, materials=mats, node_width=2) as s2, rt.Scene(tris, materials=mats, node_width=4) as s4:
+        a = gpu_render(rt, cuda, s2, ubo, w, h, spp, **kw)
+        b = gpu_render(rt, cuda, s4, ubo, w, h, spp, **kw)
+        c = gpu_render(rt, cuda, s4, ubo, w, h, 1, calls=spp, **kw)
+    assert np.array_equal(a, b)
+    assert np.array_equal(b, c)
+    if mode == "extended":
+        assert a[0::4].max() > 0.1
+
+
+def test_depth_zero_advances_rng_only(rt, cuda):
+    """maxRayTraceDepth 0: rayColor returns black, but every sample still
+    advances the alpha carry (raytraceBVH.comp:350-372)."""
+    tris, mats = lit_scene(rt)
+    ubo = rt.make_ubo((0.0, 0.5, 4.0), (0.0, 0.0, 0.0), depth=0, random_state=5)
+    with rt.Scene(tris, materials=mats, node_width=2) as s2, rt.Scene(tris, materials=mats, node_width=4) as s4:
+        a = gpu_render(rt, cuda, s2, ubo, 40, 20, 3)
+        b = gpu_render(rt, cuda, s4, ubo, 40, 20, 3)
+    assert np.array_equal(a, b)
+    px = a.reshape(-1, 4)
+    assert np.all(px[:, :3] == 0.0)
+    assert np.all(px[:, 3] != 1.0)
