@@ -67,6 +67,7 @@ def parse():
     p.add_argument("--no-batched", action="store_true", help="skip the config-4 batched comparison")
     p.add_argument("--no-served", action="store_true", help="skip the config-5 serving run")
     p.add_argument("--no-render", action="store_true", help="skip the config-2 path-tracing run")
+    p.add_argument("--render-spp", type=int, default=16, help="samples per pixel of the config-2 frame")
     p.add_argument("--serve-requests", type=int, default=200)
     p.add_argument("--serve-rates", type=str, default="1000,4000,8000", help="Poisson arrival rates (requests/s)")
     return p.parse_args()
@@ -185,12 +186,18 @@ def cpu_leg(tris, nodes, rays, sample: int) -> tuple[dict, dict]:
     ref_hits, st = orc.trace(S, sub, canonical=False, nthreads=cores)
     dt = time.perf_counter() - t0
     cnt = np.ascontiguousarray(rays[:COUNT_SAMPLE])
+    t1 = time.perf_counter()
     can_hits, cst = orc.trace(S, cnt, canonical=True, nthreads=cores)
+    dt_can = time.perf_counter() - t1
     counts = {"node_boxes_per_ray": float(cst[0]) / len(cnt), "tri_tests_per_ray": float(cst[1]) / len(cnt),
               "sample": len(cnt)}
     base = {"value": len(sub) / dt / 1e9, "unit": UNIT, "cores": cores, "kind": "port",
             "sample": f"first {len(sub)} rays of the config-3 batch, oracle restatement of hitBVH "
-                      f"(reference order, no culling, sorted-leaf BVH), {cores} threads, {dt:.2f} s"}
+                      f"(reference order, no culling, sorted-leaf BVH), {cores} threads, {dt:.2f} s",
+            "canonical": {"value": len(cnt) / dt_can / 1e9, "unit": UNIT, "cores": cores,
+                          "sample": f"first {len(cnt)} rays, the same restatement with near-child-first "
+                                    f"order and interval culling (the kernels' order; same hits), "
+                                    f"{dt_can:.2f} s"}}
     return base, {"counts": counts, "ref_hits": ref_hits, "can_hits": can_hits}
 
 
@@ -277,27 +284,41 @@ def run_extras(torch, rt, scene, tris, d_rays, n: int) -> dict:
     return out
 
 
-def run_render(torch, rt) -> dict:
+def run_render(torch, rt, spp: int = 16) -> dict:
     """Config 2: 64 displaced icospheres (subdiv 6), 1280x720, 16 samples,
     depth 8, one rt_render call (all samples), extended shading (metal,
     dielectric, sky colour) and reference shading."""
     tris, mats = rt.gen_spheres_scene(2, 64, 6, 0.05)
-    w, h, spp = 1280, 720, 16
+    w, h = 1280, 720
     ubo = rt.make_ubo((0.0, 3.0, 28.0), (0.0, 0.0, 0.0), fov=40.0, depth=8, random_state=2,
                       num_triangles=len(tris), num_materials=len(mats))
     out = {"workload": "config 2: 64 icospheres subdiv 6 (5,242,880 triangles), radial value-noise displacement "
-                       "0.05, lambertian/metal/dielectric, 1280x720, 16 spp, depth 8",
+                       f"0.05, lambertian/metal/dielectric, 1280x720, {spp} spp, depth 8",
            "triangles": int(len(tris)), "paths": w * h * spp, "unit": "Mpaths/s"}
     with rt.Scene(tris, materials=mats) as sc:
         acc = torch.empty(w * h * 4, dtype=torch.float32, device="cuda")
         for mode, name in ((rt.SHADE_EXTENDED, "extended"), (rt.SHADE_REFERENCE, "reference")):
-            def frame():
+            for every in (False, True):
+                def frame():
+                    rt.accum_clear(acc, w, h)
+                    sc.render(ubo, acc, w, h, spp, shade_mode=mode, background=(0.6, 0.7, 1.0),
+                              trace_every_primary=every)
+                ms = _time_events(torch, frame, warmup=1, reps=3)
+                img = acc.cpu().numpy().reshape(h, w, 4)
                 rt.accum_clear(acc, w, h)
-                sc.render(ubo, acc, w, h, spp, shade_mode=mode, background=(0.6, 0.7, 1.0))
-            ms = _time_events(torch, frame, warmup=1, reps=3)
-            img = acc.cpu().numpy().reshape(h, w, 4)
-            out[name] = {"value": w * h * spp / ms / 1e3, "ms_per_frame": ms,
-                         "mean_rgb": [float(img[..., k].mean() / spp) for k in range(3)]}
+                q, nodes, prims = sc.render_count(ubo, acc, w, h, spp, shade_mode=mode, background=(0.6, 0.7, 1.0),
+                                                  trace_every_primary=every)
+                r = {"value": w * h * spp / ms / 1e3, "ms_per_frame": ms,
+                     "mean_rgb": [float(img[..., k].mean() / spp) for k in range(3)],
+                     "queries_per_path": q / (w * h * spp), "Gqueries_per_s": q / ms / 1e6,
+                     "nodes_per_query": nodes / max(q, 1), "prims_per_query": prims / max(q, 1)}
+                if every:
+                    r["note"] = "every sample traces its primary ray, as the reference's spp dispatches do"
+                    out[name]["every_sample_traces_primary"] = r
+                else:
+                    r["note"] = ("default: a pixel's first hit is found once and shared by its samples (no camera "
+                                 "jitter, so every sample starts with the same ray); the image is the same bit for bit")
+                    out[name] = r
     return out
 
 
@@ -493,7 +514,7 @@ def run_ours(args):
         return
     extras = run_extras(torch, rt, scene, tris, d_rays, n) if (args.tris, args.rays) == (N_TRIS, N_RAYS) else None
     batched = None if args.no_batched else run_batched(torch, rt)
-    render = None if args.no_render else run_render(torch, rt)
+    render = None if args.no_render else run_render(torch, rt, args.render_spp)
     served = None if args.no_served else run_served(
         torch, rt, args.serve_requests, [float(x) for x in args.serve_rates.split(",") if x])
     peak, peak_kind = measured_peak()

@@ -393,9 +393,18 @@ enum {
   RT_SHADE_EXTENDED = 1   /* + metal (fuzz), dielectric (ior), background colour */
 };
 
+/* RtRenderOptions.flags.  The reference camera has no jitter
+ * (raytraceBVH.comp:329-342), so every sample of a pixel starts with the same
+ * primary ray and meets the same first hit; by default the first hit is found
+ * once per pixel and call and shared by the pixel's samples (the result is the
+ * same bit for bit).  This flag traces every sample's primary ray instead, as
+ * the reference's spp dispatches do. */
+#define RT_RENDER_TRACE_EVERY_PRIMARY 1u
+
 typedef struct RtRenderOptions {
   uint32_t shade_mode;     /* RT_SHADE_REFERENCE | RT_SHADE_EXTENDED */
   float background[3];     /* used by RT_SHADE_EXTENDED only */
+  uint32_t flags;          /* RT_RENDER_TRACE_EVERY_PRIMARY or 0 */
 } RtRenderOptions;
 
 /* The S2 pass (RaytracerBVH.cpp:998-1078): spp samples per pixel of
@@ -405,6 +414,13 @@ typedef struct RtRenderOptions {
 rt_status rt_render(rt_scene* scene, const RtRaytraceUBO* ubo, float* d_accum,
                     uint32_t width, uint32_t height, uint32_t spp,
                     const RtRenderOptions* opt, void* stream);
+/* rt_render plus work counters, for measurement (no counterpart in the
+ * reference): h_counts[0] = closest-hit queries (bounces traced),
+ * h_counts[1] = inner BVH nodes fetched, h_counts[2] = primitives tested,
+ * summed over the frame.  Synchronous. */
+rt_status rt_render_count(rt_scene* scene, const RtRaytraceUBO* ubo, float* d_accum,
+                          uint32_t width, uint32_t height, uint32_t spp,
+                          const RtRenderOptions* opt, void* stream, uint64_t* h_counts);
 /* The per-frame clear of the accumulator to (0,0,0,1) (RaytracerBVH.cpp:772-776). */
 rt_status rt_accum_clear(float* d_accum, uint32_t width, uint32_t height, void* stream);
 /* The present pass's colour math, clamp(sqrt(sum/spp), 0, 1)

@@ -118,7 +118,10 @@ class RequestResult(C.Structure):
 
 
 class _RenderOptions(C.Structure):
-    _fields_ = [("shade_mode", C.c_uint32), ("background", C.c_float * 3)]
+    _fields_ = [("shade_mode", C.c_uint32), ("background", C.c_float * 3), ("flags", C.c_uint32)]
+
+
+RENDER_TRACE_EVERY_PRIMARY = 1
 
 
 assert C.sizeof(RaytracingUBO) == 80
@@ -140,6 +143,8 @@ SIGNATURES = {
     "rt_trace_host": (_I, [_P, _P, _U32, _P, _U32, _P]),
     "rt_trace_count": (_I, [_P, _P, _U32, _P, _U32, _P, C.POINTER(_U64)]),
     "rt_render": (_I, [_P, C.POINTER(RaytracingUBO), _P, _U32, _U32, _U32, C.POINTER(_RenderOptions), _P]),
+    "rt_render_count": (_I, [_P, C.POINTER(RaytracingUBO), _P, _U32, _U32, _U32, C.POINTER(_RenderOptions), _P,
+                             C.POINTER(_U64)]),
     "rt_accum_clear": (_I, [_P, _U32, _U32, _P]),
     "rt_resolve": (_I, [_P, _U32, _U32, _U32, _P, _P]),
     "rt_last_error_string": (C.c_char_p, []),
@@ -303,11 +308,26 @@ class Scene:
         return out
 
     def render(self, ubo: RaytracingUBO, accum, width: int, height: int, spp: int,
-               shade_mode: int = SHADE_REFERENCE, background=(0.0, 0.0, 0.0), stream=None) -> None:
-        """accum: device float32 tensor of width*height*4 (RGBA32F, alpha = RNG carry)."""
-        opt = _RenderOptions(shade_mode, (C.c_float * 3)(*background))
+               shade_mode: int = SHADE_REFERENCE, background=(0.0, 0.0, 0.0), stream=None,
+               trace_every_primary: bool = False) -> None:
+        """accum: device float32 tensor of width*height*4 (RGBA32F, alpha = RNG carry).
+        trace_every_primary: trace each sample's primary ray instead of sharing a
+        pixel's first hit between its samples (same result)."""
+        opt = _RenderOptions(shade_mode, (C.c_float * 3)(*background),
+                             RENDER_TRACE_EVERY_PRIMARY if trace_every_primary else 0)
         _check(lib().rt_render(self.handle, C.byref(ubo), _ptr(accum), width, height, spp, C.byref(opt),
                                _stream_handle(stream)), "rt_render")
+
+    def render_count(self, ubo: RaytracingUBO, accum, width: int, height: int, spp: int,
+                     shade_mode: int = SHADE_REFERENCE, background=(0.0, 0.0, 0.0), stream=None,
+                     trace_every_primary: bool = False) -> tuple[int, int, int]:
+        """render with work counters -> (closest-hit queries traced, inner nodes fetched, primitives tested)."""
+        opt = _RenderOptions(shade_mode, (C.c_float * 3)(*background),
+                             RENDER_TRACE_EVERY_PRIMARY if trace_every_primary else 0)
+        c = (_U64 * 3)()
+        _check(lib().rt_render_count(self.handle, C.byref(ubo), _ptr(accum), width, height, spp, C.byref(opt),
+                                     _stream_handle(stream), c), "rt_render_count")
+        return int(c[0]), int(c[1]), int(c[2])
 
     def close(self) -> None:
         if getattr(self, "_h", None) is not None and self._h.value:
@@ -390,6 +410,17 @@ class Pool:
                                       _stream_handle(stream), repeats), "rt_pool_autotune")
         inf = self.info()
         return inf.tuned_variant, inf.tuned_refill
+
+    def render_count(self, ubo: RaytracingUBO, accum, width: int, height: int, spp: int,
+                     shade_mode: int = SHADE_REFERENCE, background=(0.0, 0.0, 0.0), stream=None,
+                     trace_every_primary: bool = False) -> tuple[int, int, int]:
+        """render with work counters -> (closest-hit queries traced, inner nodes fetched, primitives tested)."""
+        opt = _RenderOptions(shade_mode, (C.c_float * 3)(*background),
+                             RENDER_TRACE_EVERY_PRIMARY if trace_every_primary else 0)
+        c = (_U64 * 3)()
+        _check(lib().rt_render_count(self.handle, C.byref(ubo), _ptr(accum), width, height, spp, C.byref(opt),
+                                     _stream_handle(stream), c), "rt_render_count")
+        return int(c[0]), int(c[1]), int(c[2])
 
     def close(self) -> None:
         if getattr(self, "_h", None) is not None and self._h.value:
@@ -477,6 +508,17 @@ class Server:
         if n is None:
             n = d_rays.numel() * d_rays.element_size() // RAY_DTYPE.itemsize
         _check(lib().rt_server_autotune(self.handle, scene_id, _ptr(d_rays), n, _ptr(d_hits)), "rt_server_autotune")
+
+    def render_count(self, ubo: RaytracingUBO, accum, width: int, height: int, spp: int,
+                     shade_mode: int = SHADE_REFERENCE, background=(0.0, 0.0, 0.0), stream=None,
+                     trace_every_primary: bool = False) -> tuple[int, int, int]:
+        """render with work counters -> (closest-hit queries traced, inner nodes fetched, primitives tested)."""
+        opt = _RenderOptions(shade_mode, (C.c_float * 3)(*background),
+                             RENDER_TRACE_EVERY_PRIMARY if trace_every_primary else 0)
+        c = (_U64 * 3)()
+        _check(lib().rt_render_count(self.handle, C.byref(ubo), _ptr(accum), width, height, spp, C.byref(opt),
+                                     _stream_handle(stream), c), "rt_render_count")
+        return int(c[0]), int(c[1]), int(c[2])
 
     def close(self) -> None:
         if getattr(self, "_h", None) is not None and self._h.value:

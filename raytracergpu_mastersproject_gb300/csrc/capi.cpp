@@ -4,6 +4,7 @@
 // device form (see rt_internal.h) and a host copy of its reference-layout
 // nodes.  Per-stream work counters (the persistent kernels' ray/pixel
 // queues) live in a small per-(device, stream) workspace created on first use.
+#include <algorithm>
 #include <chrono>
 #include <cstdlib>
 #include <cstring>
@@ -49,6 +50,9 @@ struct Workspace {
   cudaStream_t copy_in = nullptr, copy_out = nullptr;
   cudaStream_t trace2 = nullptr;  // second trace stream of rt_trace_host
   cudaEvent_t ev[8] = {};
+  // path state and ray lists of the wavefront renderer
+  void* wave = nullptr;
+  size_t wave_bytes = 0;
 };
 static std::mutex g_ws_mu;
 static std::map<std::pair<int, cudaStream_t>, Workspace*> g_ws;
@@ -523,23 +527,29 @@ rt_status rt_trace_host(rt_scene* scene, const RtRay* h_rays, uint32_t n, RtHit*
   return RT_OK;
 }
 
-rt_status rt_render(rt_scene* scene, const RtRaytraceUBO* ubo, float* d_accum, uint32_t width, uint32_t height,
-                    uint32_t spp, const RtRenderOptions* opt, void* stream) {
+static rt_status render_impl(rt_scene* scene, const RtRaytraceUBO* ubo, float* d_accum, uint32_t width,
+                             uint32_t height, uint32_t spp, const RtRenderOptions* opt, void* stream,
+                             uint64_t* h_counts, const char* who) {
   if (!scene || !ubo || !d_accum || width == 0 || height == 0 || (uint64_t)width * height > 0x40000000ull) {
-    set_error("rt_render: bad argument");
+    set_error(std::string(who) + ": bad argument");
     return RT_EINVAL;
   }
   if (scene->max_material > scene->d.n_mats) {
-    set_error("rt_render: a primitive names a material index >= num_materials");
+    set_error(std::string(who) + ": a primitive names a material index >= num_materials");
     return RT_EINVAL;
   }
   RtRenderOptions o;
   std::memset(&o, 0, sizeof(o));
   if (opt) o = *opt;
   if (o.shade_mode != RT_SHADE_REFERENCE && o.shade_mode != RT_SHADE_EXTENDED) {
-    set_error("rt_render: unknown shade_mode");
+    set_error(std::string(who) + ": unknown shade_mode");
     return RT_EINVAL;
   }
+  if (o.flags & ~RT_RENDER_TRACE_EVERY_PRIMARY) {
+    set_error(std::string(who) + ": unknown flags");
+    return RT_EINVAL;
+  }
+  if (h_counts) h_counts[0] = h_counts[1] = h_counts[2] = 0;
   if (spp == 0) return RT_OK;
   cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
   Workspace* w = nullptr;
@@ -547,12 +557,59 @@ rt_status rt_render(rt_scene* scene, const RtRaytraceUBO* ubo, float* d_accum, u
   if (s != RT_OK) return s;
   float cam[12];
   camera_setup(*ubo, width, height, cam);
-  cudaError_t e = cudaMemsetAsync(w->counters, 0, 2 * sizeof(uint32_t), st);
+  // Paths in flight of the wavefront renderer: the whole frame up to 16 Mi
+  // paths (about 1.9 GB of scratch); larger frames run in passes.
+  static const uint64_t kMaxWavePaths = [] {
+    const char* v = std::getenv("RT_RENDER_WAVE_PATHS");
+    const long long x = v ? std::atoll(v) : 0;
+    return x >= 1 && x <= (1ll << 30) ? (uint64_t)x : (uint64_t)1 << 24;
+  }();
+  uint64_t wave_paths = 0;
+  if (render_uses_scratch(scene->d, ubo->maxRayTraceDepth)) {
+    wave_paths = std::min<uint64_t>((uint64_t)width * height * spp, kMaxWavePaths);
+    const size_t need = render_scratch_bytes(wave_paths, ubo->maxRayTraceDepth);
+    if (w->wave_bytes < need) {
+      if (w->wave) cudaFree(w->wave);
+      w->wave = nullptr;
+      w->wave_bytes = 0;
+      cudaError_t e = cudaMalloc(&w->wave, need);
+      if (e != cudaSuccess) {
+        set_error(std::string(who) + ": wavefront scratch cudaMalloc: " + cudaGetErrorString(e));
+        return RT_ENOMEM;
+      }
+      w->wave_bytes = need;
+    }
+  }
+  cudaError_t e = cudaMemsetAsync(w->counters, 0, (h_counts ? 16 : 2) * sizeof(uint32_t), st);
   if (e != cudaSuccess) return cuda_fail(e, "rt_render: memset");
-  e = launch_render(scene->d, cam, ubo->maxRayTraceDepth, ubo->randomState, d_accum, width, height, spp, o.shade_mode,
-                    o.background, w->counters, stream);
+  unsigned long long* stats = h_counts ? reinterpret_cast<unsigned long long*>(w->counters + 8) : nullptr;
+  const uint32_t mode = (o.shade_mode == RT_SHADE_EXTENDED ? kRenderExtended : 0u) |
+                        ((o.flags & RT_RENDER_TRACE_EVERY_PRIMARY) ? kRenderTraceEveryPrimary : 0u);
+  e = launch_render(scene->d, cam, ubo->maxRayTraceDepth, ubo->randomState, d_accum, width, height, spp, mode,
+                    o.background, w->counters, stream, stats, w->wave, wave_paths);
   if (e != cudaSuccess) return cuda_fail(e, "rt_render: launch");
+  if (h_counts) {
+    unsigned long long hc[3] = {0, 0, 0};
+    e = cudaMemcpyAsync(hc, stats, sizeof(hc), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return cuda_fail(e, "rt_render_count: read counters");
+    for (int k = 0; k < 3; ++k) h_counts[k] = hc[k];
+  }
   return RT_OK;
+}
+
+rt_status rt_render(rt_scene* scene, const RtRaytraceUBO* ubo, float* d_accum, uint32_t width, uint32_t height,
+                    uint32_t spp, const RtRenderOptions* opt, void* stream) {
+  return render_impl(scene, ubo, d_accum, width, height, spp, opt, stream, nullptr, "rt_render");
+}
+
+rt_status rt_render_count(rt_scene* scene, const RtRaytraceUBO* ubo, float* d_accum, uint32_t width, uint32_t height,
+                          uint32_t spp, const RtRenderOptions* opt, void* stream, uint64_t* h_counts) {
+  if (!h_counts) {
+    set_error("rt_render_count: bad argument");
+    return RT_EINVAL;
+  }
+  return render_impl(scene, ubo, d_accum, width, height, spp, opt, stream, h_counts, "rt_render_count");
 }
 
 rt_status rt_accum_clear(float* d_accum, uint32_t width, uint32_t height, void* stream) {

@@ -5,12 +5,15 @@
 // them (RaytracerBVH.cpp:1025-1050); a pixel's sample s+1 depends only on that
 // pixel's accumulator after sample s (the RNG carry lives in alpha), so here
 // one lane runs a pixel's samples back to back and the accumulator is read
-// and written once.  Two kernels: k_render_step (4-wide trees; one traversal
-// or shading step per lane per iteration, idle lanes refilled with new
-// pixels) and k_render (binary trees, or depth 0; persistent warps take 32
-// pixels at a time and run whole traversals).
+// and written once.  Three schedules: the wavefront renderer (4-wide trees,
+// the default: each bounce level traced by the ray-query step kernel, then
+// shaded in its own pass), k_render_step (4-wide trees; one traversal or
+// shading step per lane per iteration, idle lanes refilled with new pixels)
+// and k_render (binary trees, or depth 0; persistent warps take 32 pixels at
+// a time and run whole traversals).
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstdlib>
 #include <type_traits>
 
@@ -165,9 +168,9 @@ __device__ __forceinline__ bool bounce(const DeviceScene& S, const dev::Trav& s,
 }
 
 // rayColor with the whole traversal of each bounce in one call.
-template <int W, int STACK, typename StackT>
+template <int W, int STACK, typename StackT, typename WC>
 __device__ f3 ray_color(const DeviceScene& S, f3 o, f3 d, uint32_t depth, uint32_t& rng, bool extended, f3 bg,
-                        StackT* stack, uint32_t& status) {
+                        StackT* stack, uint32_t& status, WC& wc) {
   f3 color = mk(0.0f, 0.0f, 0.0f);
   f3 gatt = mk(1.0f, 1.0f, 1.0f);
   f3 co = o, cd = normalize(d);
@@ -180,6 +183,7 @@ __device__ f3 ray_color(const DeviceScene& S, f3 o, f3 d, uint32_t depth, uint32
     } else {
       dev::trav_run_wide<false, STACK>(S, s, stack, 0);
     }
+    wc.add(s);
     if (!bounce(S, s, co, cd, color, gatt, rng, extended, bg, status)) break;
   }
   return color;
@@ -191,11 +195,37 @@ __device__ __forceinline__ uint32_t lanemask_lt() {
   return m;
 }
 
-template <int W, int STACK>
+// Work counters of rt_render_count: closest-hit queries, inner nodes fetched,
+// primitives tested.  Kernels without STATS never store them, so the adds
+// are dead code there.
+struct WorkCount {
+  unsigned long long queries = 0, nodes = 0, prims = 0;
+  __device__ __forceinline__ void add(const dev::Trav& s) {
+    queries += 1;
+    nodes += s.nvis;
+    prims += s.ntest;
+  }
+  __device__ __forceinline__ void flush(unsigned long long* stats) {
+    for (int o = 16; o > 0; o >>= 1) {
+      queries += __shfl_down_sync(0xFFFFFFFFu, queries, o);
+      nodes += __shfl_down_sync(0xFFFFFFFFu, nodes, o);
+      prims += __shfl_down_sync(0xFFFFFFFFu, prims, o);
+    }
+    if ((threadIdx.x & 31u) == 0u) {
+      atomicAdd(&stats[0], queries);
+      atomicAdd(&stats[1], nodes);
+      atomicAdd(&stats[2], prims);
+    }
+  }
+};
+
+template <int W, int STACK, bool STATS>
 __global__ void __launch_bounds__(kThreads) k_render(DeviceScene S, Cam cam, uint32_t depth, uint32_t random_state,
                                                      float4* __restrict__ accum, uint32_t Wd, uint32_t H, uint32_t spp,
-                                                     uint32_t extended, float bgx, float bgy, float bgz,
-                                                     uint32_t* __restrict__ counter) {
+                                                     uint32_t mode, float bgx, float bgy, float bgz,
+                                                     uint32_t* __restrict__ counter,
+                                                     unsigned long long* __restrict__ stats) {
+  WorkCount wc;
   using StackT = typename std::conditional<W == 2, uint32_t, uint2>::type;
   StackT stack[STACK];
   const uint32_t total = Wd * H;
@@ -221,7 +251,7 @@ __global__ void __launch_bounds__(kThreads) k_render(DeviceScene S, Cam cam, uin
         const float next = rng_next(rng);                     // :352 (:351 is a no-op)
         const f3 sample = add(add(p00, scale(pdu, (float)x)), scale(pdv, (float)y));
         const f3 d = normalize(sub(sample, pos));
-        const f3 c = ray_color<W, STACK>(S, pos, d, depth, rng, extended != 0u, bg, stack, status);
+        const f3 c = ray_color<W, STACK>(S, pos, d, depth, rng, (mode & kRenderExtended) != 0u, bg, stack, status, wc);
         px.x = c.x + px.x;
         px.y = c.y + px.y;
         px.z = c.z + px.z;
@@ -231,6 +261,7 @@ __global__ void __launch_bounds__(kThreads) k_render(DeviceScene S, Cam cam, uin
     }
   }
   if (status) atomicOr(counter + 1, status);
+  if constexpr (STATS) wc.flush(stats);
 }
 
 // 4-wide trees: every lane is a small state machine that makes one move per
@@ -242,11 +273,12 @@ __global__ void __launch_bounds__(kThreads) k_render(DeviceScene S, Cam cam, uin
 // samples in order, so the accumulator sums are the same as k_render's.  Each
 // phase's code appears once in the loop, which keeps the kernel small enough
 // for the instruction cache.
-template <int STACK, int THREADS, int MINB>
+template <int STACK, int THREADS, int MINB, bool STATS>
 __global__ void __launch_bounds__(THREADS, MINB)
     k_render_step(DeviceScene S, Cam cam, uint32_t depth, uint32_t random_state, float4* __restrict__ accum,
-                  uint32_t Wd, uint32_t H, uint32_t spp, uint32_t extended, float bgx, float bgy, float bgz,
-                  uint32_t* __restrict__ counter, int refill) {
+                  uint32_t Wd, uint32_t H, uint32_t spp, uint32_t mode, float bgx, float bgy, float bgz,
+                  uint32_t* __restrict__ counter, int refill, unsigned long long* __restrict__ stats) {
+  WorkCount wc;
   enum : uint32_t { kIdle, kTraverse, kShade, kNewSample };
   uint2 stack[STACK];
   dev::Trav s;
@@ -254,8 +286,13 @@ __global__ void __launch_bounds__(THREADS, MINB)
   const uint32_t lane = threadIdx.x & 31u;
   const f3 bg = mk(bgx, bgy, bgz);
   const int min_idle = refill < 1 ? 1 : (refill > 32 ? 32 : refill);
+  const bool extended = (mode & kRenderExtended) != 0u;
+  const bool share = (mode & kRenderTraceEveryPrimary) == 0u;
   uint32_t status = 0;
   uint32_t phase = kIdle, pix = 0, smp = 0, nb = 0, rng = 0;
+  uint32_t first_best = 0;  // the pixel's first hit (sample 0, bounce 0)
+  float first_t = 0.0f;
+  int first_sp = 0;
   float4 px = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
   f3 color = mk(0.0f, 0.0f, 0.0f), gatt = mk(1.0f, 1.0f, 1.0f), co = color, cd = color;
   bool exhausted = spp == 0u;
@@ -289,7 +326,13 @@ __global__ void __launch_bounds__(THREADS, MINB)
     }
     bool trace = false;
     if (phase == kShade) {
-      if (bounce(S, s, co, cd, color, gatt, rng, extended != 0u, bg, status) && ++nb < depth) {
+      if (nb == 0u && smp == 0u) {  // keep the pixel's first hit for its later samples
+        first_best = s.best;
+        first_t = s.tclose;
+        first_sp = s.sp;
+      }
+      if (STATS && (nb != 0u || smp == 0u || !share)) wc.add(s);
+      if (bounce(S, s, co, cd, color, gatt, rng, extended, bg, status) && ++nb < depth) {
         trace = true;
       } else {  // the sample is done
         px.x = color.x + px.x;
@@ -317,7 +360,14 @@ __global__ void __launch_bounds__(THREADS, MINB)
       co = pos;
       cd = normalize(d);
       nb = 0;
-      trace = true;  // depth >= 1 (the launcher sends depth 0 to k_render)
+      if (share && smp > 0u) {  // the same primary ray: its first hit is known
+        s.best = first_best;
+        s.tclose = first_t;
+        s.sp = first_sp < 0 ? -1 : 0;
+        phase = kShade;
+      } else {
+        trace = true;  // depth >= 1 (the launcher sends depth 0 to k_render)
+      }
     }
     if (trace) {
       dev::trav_init_ray(s, make_float4(co.x, co.y, co.z, 0.001f), make_float4(cd.x, cd.y, cd.z, 10000000.0f), S.root);
@@ -329,6 +379,200 @@ __global__ void __launch_bounds__(THREADS, MINB)
     }
   }
   if (status) atomicOr(counter + 1, status);
+  if constexpr (STATS) wc.flush(stats);
+}
+
+// ---------------------------------------------------------- wavefront ----
+// 4-wide trees: the frame runs level by level (bounce 0, 1, ...).  Each level
+// traces all of its rays with the ray-query step kernel (RAW hits) and then
+// shades them in a separate pass, one path per thread, which appends the
+// continuing paths and their next rays to the next level's list.  Traversal
+// and shading thus each run with the lanes of a warp doing the same kind of
+// work.  A path's RNG state starts from the pixel's alpha carry chain, which
+// needs no tracing (k_wave_seed), and each pixel adds its samples' colours in
+// sample order at the end (k_wave_accum), so the accumulator is the same as
+// with one lane running the pixel's samples back to back.
+//
+// Scratch per path: state (color.xyz, rng | gatt.xyz, -) 32 B, two ray
+// buffers 2 x 32 B, two path lists 2 x 4 B, hits 8 B.
+struct WaveBufs {
+  float4* state;  // 2 float4 per path
+  float4* rays[2];
+  uint32_t* list[2];
+  uint2* hits;
+  uint32_t* cnt;  // 4 words per level: trace queue, -, ray count, -
+};
+
+__global__ void k_wave_seed(Cam cam, uint32_t random_state, float4* __restrict__ accum, uint32_t Wd, uint32_t pix0,
+                            uint32_t npix, uint32_t ns, uint32_t per_path, float4* __restrict__ state,
+                            float4* __restrict__ rays) {
+  for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < npix; q += gridDim.x * blockDim.x) {
+    const uint32_t pix = pix0 + q;
+    const uint32_t x = pix % Wd, y = pix / Wd;
+    float4 px = accum[pix];
+    for (uint32_t k = 0; k < ns; ++k) {
+      uint32_t rng = (600u * x + y) * (random_state + 1u);  // random.glsl:9
+      rng += __float2uint_rz(px.w * 4294967294.0f);         // raytraceBVH.comp:350, saturating
+      px.w = rng_next(rng);                                 // :352 (:351 is a no-op)
+      const size_t p = (size_t)q * ns + k;
+      state[2 * p] = make_float4(0.0f, 0.0f, 0.0f, __uint_as_float(rng));
+      state[2 * p + 1] = make_float4(1.0f, 1.0f, 1.0f, 0.0f);
+    }
+    accum[pix] = px;  // the carry after these samples; the colours are added by k_wave_accum
+    const f3 pos = mk(cam.v[0], cam.v[1], cam.v[2]);
+    const f3 sample = add(add(mk(cam.v[3], cam.v[4], cam.v[5]), scale(mk(cam.v[6], cam.v[7], cam.v[8]), (float)x)),
+                          scale(mk(cam.v[9], cam.v[10], cam.v[11]), (float)y));
+    const f3 cd = normalize(normalize(sub(sample, pos)));  // getRay, then rayColor's normalize
+    const float4 o = make_float4(pos.x, pos.y, pos.z, 0.001f);
+    const float4 d = make_float4(cd.x, cd.y, cd.z, 10000000.0f);
+    if (per_path) {
+      for (uint32_t k = 0; k < ns; ++k) {
+        const size_t p = (size_t)q * ns + k;
+        rays[2 * p] = o;
+        rays[2 * p + 1] = d;
+      }
+    } else {
+      rays[2 * (size_t)q] = o;
+      rays[2 * (size_t)q + 1] = d;
+    }
+  }
+}
+
+// Shades level `level`: n0 rays at level 0 (path p's ray is rays[p] or, when
+// the pixel's first hit is shared, rays[p / ns]); later levels take the count
+// from the level's counter block and path ids from `list`.
+template <bool STATS>
+__global__ void k_wave_shade(DeviceScene S, uint32_t level, uint32_t depth, uint32_t n0, uint32_t ns, uint32_t per_path,
+                             uint32_t mode, float bgx, float bgy, float bgz, float4* __restrict__ state,
+                             const float4* __restrict__ rays, const uint32_t* __restrict__ list,
+                             const uint2* __restrict__ hits, float4* __restrict__ next_rays,
+                             uint32_t* __restrict__ next_list, uint32_t* __restrict__ cnt,
+                             uint32_t* __restrict__ status_word, unsigned long long* __restrict__ stats) {
+  const uint32_t n = level == 0 ? n0 : *reinterpret_cast<volatile uint32_t*>(cnt + 4u * level + 2u);
+  if (STATS && level == 0 && blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&stats[0], (unsigned long long)(per_path ? n0 : n0 / ns));
+  if (STATS && level > 0 && blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&stats[0], (unsigned long long)n);
+  const bool extended = (mode & kRenderExtended) != 0u;
+  const f3 bg = mk(bgx, bgy, bgz);
+  uint32_t status = 0;
+  const uint32_t stride = gridDim.x * blockDim.x;
+  for (uint32_t i0 = blockIdx.x * blockDim.x; i0 < n; i0 += stride) {  // warp-uniform trip count
+    const uint32_t i = i0 + threadIdx.x;
+    bool more = false;
+    uint32_t p = 0;
+    f3 co = mk(0.0f, 0.0f, 0.0f), cd = co;
+    if (i < n) {
+      p = level == 0 ? i : list[i];
+      const uint32_t r = level == 0 ? (per_path ? i : i / ns) : i;
+      const float4 o = rays[2 * (size_t)r], d = rays[2 * (size_t)r + 1];
+      const uint2 h = hits[r];
+      dev::Trav s;
+      s.best = h.x == kRawOverflow ? 0u : h.x;
+      s.sp = h.x == kRawOverflow ? -1 : 0;
+      s.tclose = __uint_as_float(h.y);
+      float4 a = state[2 * (size_t)p], g = state[2 * (size_t)p + 1];
+      f3 color = mk(a.x, a.y, a.z), gatt = mk(g.x, g.y, g.z);
+      uint32_t rng = __float_as_uint(a.w);
+      co = mk(o.x, o.y, o.z);
+      cd = mk(d.x, d.y, d.z);
+      more = bounce(S, s, co, cd, color, gatt, rng, extended, bg, status) && level + 1u < depth;
+      state[2 * (size_t)p] = make_float4(color.x, color.y, color.z, __uint_as_float(rng));
+      state[2 * (size_t)p + 1] = make_float4(gatt.x, gatt.y, gatt.z, 0.0f);
+    }
+    // append the continuing paths: one atomicAdd per warp
+    const uint32_t m = __ballot_sync(0xFFFFFFFFu, more);
+    if (m) {
+      const uint32_t lane = threadIdx.x & 31u;
+      uint32_t base = 0;
+      if (lane == (uint32_t)(__ffs(m) - 1)) base = atomicAdd(cnt + 4u * (level + 1u) + 2u, (uint32_t)__popc(m));
+      base = __shfl_sync(0xFFFFFFFFu, base, __ffs(m) - 1);
+      if (more) {
+        const uint32_t j = base + (uint32_t)__popc(m & lanemask_lt());
+        next_list[j] = p;
+        next_rays[2 * (size_t)j] = make_float4(co.x, co.y, co.z, 0.001f);
+        next_rays[2 * (size_t)j + 1] = make_float4(cd.x, cd.y, cd.z, 10000000.0f);
+      }
+    }
+  }
+  if (status) atomicOr(status_word, status);
+}
+
+__global__ void k_wave_accum(float4* __restrict__ accum, uint32_t pix0, uint32_t npix, uint32_t ns,
+                             const float4* __restrict__ state) {
+  for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < npix; q += gridDim.x * blockDim.x) {
+    float4 px = accum[pix0 + q];
+    for (uint32_t k = 0; k < ns; ++k) {
+      const float4 c = state[2 * ((size_t)q * ns + k)];
+      px.x = c.x + px.x;
+      px.y = c.y + px.y;
+      px.z = c.z + px.z;
+    }
+    accum[pix0 + q] = px;
+  }
+}
+
+constexpr size_t kWaveBytesPerPath = 32 + 64 + 8 + 8;
+// Two launches per level: deeper paths go to k_render_step instead.
+constexpr uint32_t kWaveMaxDepth = 64;
+
+WaveBufs wave_bufs(void* scratch, uint64_t paths, uint32_t depth) {
+  auto up = [](size_t v) { return (v + 255) & ~(size_t)255; };
+  char* b = static_cast<char*>(scratch);
+  WaveBufs w;
+  size_t off = 0;
+  w.state = reinterpret_cast<float4*>(b + off);
+  off += up(paths * 32);
+  w.rays[0] = reinterpret_cast<float4*>(b + off);
+  off += up(paths * 32);
+  w.rays[1] = reinterpret_cast<float4*>(b + off);
+  off += up(paths * 32);
+  w.list[0] = reinterpret_cast<uint32_t*>(b + off);
+  off += up(paths * 4);
+  w.list[1] = reinterpret_cast<uint32_t*>(b + off);
+  off += up(paths * 4);
+  w.hits = reinterpret_cast<uint2*>(b + off);
+  off += up(paths * 8);
+  w.cnt = reinterpret_cast<uint32_t*>(b + off);
+  (void)depth;
+  return w;
+}
+
+template <bool STATS>
+cudaError_t launch_render_wave(const DeviceScene& S, const Cam& cam, uint32_t depth, uint32_t rs, float* accum_f,
+                               uint32_t Wd, uint32_t H, uint32_t spp, uint32_t mode, const float bg[3],
+                               uint32_t* counter, unsigned long long* stats, void* scratch, uint64_t max_paths,
+                               cudaStream_t st) {
+  float4* accum = reinterpret_cast<float4*>(accum_f);
+  const uint32_t total = Wd * H;
+  const uint32_t per_path = (mode & kRenderTraceEveryPrimary) ? 1u : 0u;
+  const uint32_t ns_pass = (uint32_t)std::min<uint64_t>(spp, max_paths);
+  const uint32_t q_chunk = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(total, max_paths / ns_pass));
+  const WaveBufs B = wave_bufs(scratch, max_paths, depth);
+  const uint32_t sms = (uint32_t)device_sm_count();
+  unsigned long long* trace_stats = STATS ? stats + 1 : nullptr;
+  cudaError_t e;
+  for (uint32_t pix0 = 0; pix0 < total; pix0 += q_chunk) {
+    const uint32_t q = std::min(q_chunk, total - pix0);
+    for (uint32_t s0 = 0; s0 < spp; s0 += ns_pass) {
+      const uint32_t ns = std::min(ns_pass, spp - s0);
+      const uint32_t np = q * ns;
+      if ((e = cudaMemsetAsync(B.cnt, 0, 16 * ((size_t)depth + 1), st)) != cudaSuccess) return e;
+      const uint32_t gb = std::min<uint32_t>(sms * 8, (q + 255) / 256);
+      k_wave_seed<<<gb, 256, 0, st>>>(cam, rs, accum, Wd, pix0, q, ns, per_path, B.state, B.rays[0]);
+      for (uint32_t l = 0; l < depth; ++l) {
+        const float4* r = B.rays[l & 1u];
+        if ((e = launch_trace_raw(S, r, l == 0 ? (per_path ? np : q) : 0xFFFFFFFFu, B.hits, B.cnt + 4u * l,
+                                  trace_stats, st)) != cudaSuccess)
+          return e;
+        const uint32_t gs = l == 0 ? std::min<uint32_t>(sms * 8, (np + 255) / 256) : sms * 8;
+        k_wave_shade<STATS><<<gs, 256, 0, st>>>(S, l, depth, np, ns, per_path, mode, bg[0], bg[1], bg[2], B.state, r,
+                                                B.list[l & 1u], B.hits, B.rays[(l + 1u) & 1u], B.list[(l + 1u) & 1u],
+                                                B.cnt, counter + 1, stats);
+      }
+      k_wave_accum<<<gb, 256, 0, st>>>(accum, pix0, q, ns, B.state);
+      if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    }
+  }
+  return cudaGetLastError();
 }
 
 __global__ void k_clear(float4* accum, uint32_t total) {
@@ -349,13 +593,14 @@ __global__ void k_resolve(const float4* accum, uint32_t total, float inv_spp_den
   }
 }
 
-template <int W, int STACK>
+template <int W, int STACK, bool STATS>
 cudaError_t launch_render_variant(const DeviceScene& S, const Cam& cam, uint32_t depth, uint32_t rs, float* accum,
                                   uint32_t w, uint32_t h, uint32_t spp, uint32_t shade, const float bg[3],
-                                  uint32_t* counter, cudaStream_t st) {
+                                  uint32_t* counter, unsigned long long* stats, cudaStream_t st) {
   static int blocks_per_sm = -1;
   if (blocks_per_sm < 0) {
-    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, k_render<W, STACK>, kThreads, 0);
+    cudaError_t e =
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, k_render<W, STACK, STATS>, kThreads, 0);
     if (e != cudaSuccess) return e;
     if (blocks_per_sm < 1) blocks_per_sm = 1;
   }
@@ -364,18 +609,20 @@ cudaError_t launch_render_variant(const DeviceScene& S, const Cam& cam, uint32_t
   const uint32_t needed = (total + kThreads - 1) / kThreads;
   if (blocks > needed) blocks = needed;
   if (blocks == 0) blocks = 1;
-  k_render<W, STACK><<<blocks, kThreads, 0, st>>>(S, cam, depth, rs, reinterpret_cast<float4*>(accum), w, h, spp,
-                                               shade == RT_SHADE_EXTENDED ? 1u : 0u, bg[0], bg[1], bg[2], counter);
+  k_render<W, STACK, STATS><<<blocks, kThreads, 0, st>>>(S, cam, depth, rs, reinterpret_cast<float4*>(accum), w, h,
+                                                         spp, shade, bg[0], bg[1],
+                                                         bg[2], counter, stats);
   return cudaGetLastError();
 }
 
-template <int STACK, int T, int M>
+template <int STACK, int T, int M, bool STATS>
 cudaError_t launch_render_step(const DeviceScene& S, const Cam& cam, uint32_t depth, uint32_t rs, float* accum,
                                uint32_t w, uint32_t h, uint32_t spp, uint32_t shade, const float bg[3],
-                               uint32_t* counter, int refill, cudaStream_t st) {
+                               uint32_t* counter, int refill, unsigned long long* stats, cudaStream_t st) {
   static int blocks_per_sm = -1;
   if (blocks_per_sm < 0) {
-    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, k_render_step<STACK, T, M>, T, 0);
+    cudaError_t e =
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, k_render_step<STACK, T, M, STATS>, T, 0);
     if (e != cudaSuccess) return e;
     if (blocks_per_sm < 1) blocks_per_sm = 1;
   }
@@ -384,9 +631,9 @@ cudaError_t launch_render_step(const DeviceScene& S, const Cam& cam, uint32_t de
   const uint32_t needed = (total + T - 1) / T;
   if (blocks > needed) blocks = needed;
   if (blocks == 0) blocks = 1;
-  k_render_step<STACK, T, M><<<blocks, T, 0, st>>>(S, cam, depth, rs, reinterpret_cast<float4*>(accum), w, h, spp,
-                                                   shade == RT_SHADE_EXTENDED ? 1u : 0u, bg[0], bg[1], bg[2], counter,
-                                                   refill);
+  k_render_step<STACK, T, M, STATS><<<blocks, T, 0, st>>>(S, cam, depth, rs, reinterpret_cast<float4*>(accum), w, h,
+                                                          spp, shade, bg[0], bg[1],
+                                                          bg[2], counter, refill, stats);
   return cudaGetLastError();
 }
 
@@ -397,41 +644,64 @@ int env_int(const char* name, int dflt) {
 
 // 0: k_render (one thread per pixel, whole traversals); 1-3: k_render_step
 // with 128 threads and at least 8, 6 or 10 blocks per SM (6: 72 registers, no
-// spills -- the default; 8 and 10 spill).
+// spills; 8 and 10 spill); 4: the wavefront renderer (the default; depth up
+// to kWaveMaxDepth, deeper frames use variant 2).
 struct RenderTuning {
   int variant, refill;
 };
 const RenderTuning& render_tuning() {
-  static const RenderTuning t{env_int("RT_RENDER_VARIANT", 2), env_int("RT_RENDER_REFILL", 8)};
+  static const RenderTuning t{env_int("RT_RENDER_VARIANT", 4), env_int("RT_RENDER_REFILL", 8)};
   return t;
+}
+
+template <bool STATS>
+cudaError_t launch_render_impl(const DeviceScene& s, const Cam& c, uint32_t depth, uint32_t random_state, float* accum,
+                               uint32_t w, uint32_t h, uint32_t spp, uint32_t mode, const float bg[3],
+                               uint32_t* counter, unsigned long long* stats, void* scratch, uint64_t scratch_paths,
+                               cudaStream_t st) {
+  const RenderTuning& tn = render_tuning();
+  if (s.width == 4 && depth > 0u && depth <= kWaveMaxDepth && tn.variant == 4 && scratch && scratch_paths > 0)
+    return launch_render_wave<STATS>(s, c, depth, random_state, accum, w, h, spp, mode, bg, counter, stats, scratch,
+                                     scratch_paths, st);
+  if (s.width == 4 && depth > 0u && tn.variant >= 1 && tn.variant <= 4) {  // 4: depth beyond the wavefront's
+    const bool big = s.stack_need > 64u;
+#define RT_STEP(STK, T, M)                                                                                         \
+  launch_render_step<STK, T, M, STATS>(s, c, depth, random_state, accum, w, h, spp, mode, bg, counter, \
+                                       tn.refill, stats, st)
+    if (tn.variant == 2 || tn.variant == 4) return big ? RT_STEP(192, 128, 6) : RT_STEP(64, 128, 6);
+    if (tn.variant == 3) return big ? RT_STEP(192, 128, 10) : RT_STEP(64, 128, 10);
+    return big ? RT_STEP(192, 128, 8) : RT_STEP(64, 128, 8);
+#undef RT_STEP
+  }
+#define RT_PIX(W, STK) \
+  launch_render_variant<W, STK, STATS>(s, c, depth, random_state, accum, w, h, spp, mode, bg, counter, stats, st)
+  if (s.width == 4) return s.stack_need <= 64u ? RT_PIX(4, 64) : RT_PIX(4, 192);
+  return s.stack_need <= 64u ? RT_PIX(2, 64) : RT_PIX(2, 128);
+#undef RT_PIX
 }
 
 }  // namespace
 
 cudaError_t launch_render(const DeviceScene& s, const float cam[12], uint32_t depth, uint32_t random_state,
-                          float* accum, uint32_t w, uint32_t h, uint32_t spp, uint32_t shade_mode, const float bg[3],
-                          uint32_t* counter, void* stream) {
+                          float* accum, uint32_t w, uint32_t h, uint32_t spp, uint32_t mode, const float bg[3],
+                          uint32_t* counter, void* stream, unsigned long long* stats, void* scratch,
+                          uint64_t scratch_paths) {
   Cam c;
   for (int k = 0; k < 12; ++k) c.v[k] = cam[k];
   cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
-  const RenderTuning& tn = render_tuning();
-  if (s.width == 4 && depth > 0u && tn.variant >= 1 && tn.variant <= 3) {
-    const bool big = s.stack_need > 64u;
-#define RT_STEP(STK, T, M) \
-  launch_render_step<STK, T, M>(s, c, depth, random_state, accum, w, h, spp, shade_mode, bg, counter, tn.refill, st)
-    if (tn.variant == 2) return big ? RT_STEP(192, 128, 6) : RT_STEP(64, 128, 6);
-    if (tn.variant == 3) return big ? RT_STEP(192, 128, 10) : RT_STEP(64, 128, 10);
-    return big ? RT_STEP(192, 128, 8) : RT_STEP(64, 128, 8);
-#undef RT_STEP
-  }
-  if (s.width == 4) {
-    if (s.stack_need <= 64u)
-      return launch_render_variant<4, 64>(s, c, depth, random_state, accum, w, h, spp, shade_mode, bg, counter, st);
-    return launch_render_variant<4, 192>(s, c, depth, random_state, accum, w, h, spp, shade_mode, bg, counter, st);
-  }
-  if (s.stack_need <= 64u)
-    return launch_render_variant<2, 64>(s, c, depth, random_state, accum, w, h, spp, shade_mode, bg, counter, st);
-  return launch_render_variant<2, 128>(s, c, depth, random_state, accum, w, h, spp, shade_mode, bg, counter, st);
+  if (stats)
+    return launch_render_impl<true>(s, c, depth, random_state, accum, w, h, spp, mode, bg, counter, stats, scratch,
+                                    scratch_paths, st);
+  return launch_render_impl<false>(s, c, depth, random_state, accum, w, h, spp, mode, bg, counter, nullptr, scratch,
+                                   scratch_paths, st);
+}
+
+bool render_uses_scratch(const DeviceScene& s, uint32_t depth) {
+  return s.width == 4 && depth > 0u && depth <= kWaveMaxDepth && render_tuning().variant == 4;
+}
+
+size_t render_scratch_bytes(uint64_t paths, uint32_t depth) {
+  return (size_t)paths * kWaveBytesPerPath + 7 * 256 + 16 * ((size_t)depth + 1);
 }
 
 cudaError_t launch_accum_clear(float* accum, uint32_t w, uint32_t h, void* stream) {

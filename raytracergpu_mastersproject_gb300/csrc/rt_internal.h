@@ -149,9 +149,24 @@ cudaError_t launch_reorder(const DeviceScene& s, const RtRay* rays, uint32_t n, 
 // Kernels launch on the given stream; counter is a device uint32 zeroed by the caller.
 cudaError_t launch_trace(const DeviceScene& s, const RtRay* rays, uint32_t n, RtHit* hits, uint32_t flags,
                          uint32_t* counter, void* stream, const uint32_t* order = nullptr);
+// Path-tracer queries (render.cu): hits[i] = (leaf-style ref of the closest
+// primitive, 0: none, or kRawOverflow; t bits).  n == 0xFFFFFFFF takes the
+// count from counter[2]; counter[0] must be zero.
+constexpr uint32_t kRawOverflow = 0xFFFFFFFEu;
+cudaError_t launch_trace_raw(const DeviceScene& s, const float4* rays, uint32_t n, uint2* hits, uint32_t* counter,
+                             unsigned long long* stats, cudaStream_t stream);
+// launch_render mode bits
+constexpr uint32_t kRenderExtended = 1u;            // RT_SHADE_EXTENDED
+constexpr uint32_t kRenderTraceEveryPrimary = 2u;   // RT_RENDER_TRACE_EVERY_PRIMARY
 cudaError_t launch_render(const DeviceScene& s, const float cam[12], uint32_t depth, uint32_t random_state,
-                          float* accum, uint32_t w, uint32_t h, uint32_t spp, uint32_t shade_mode,
-                          const float bg[3], uint32_t* counter, void* stream);
+                          float* accum, uint32_t w, uint32_t h, uint32_t spp, uint32_t mode,
+                          const float bg[3], uint32_t* counter, void* stream,
+                          unsigned long long* stats = nullptr,  // stats: queries, nodes, primitives
+                          void* scratch = nullptr, uint64_t scratch_paths = 0);
+// The wavefront renderer (4-wide trees) needs scratch of render_scratch_bytes
+// for up to `paths` paths in flight; the frame is split into passes that fit.
+bool render_uses_scratch(const DeviceScene& s, uint32_t depth);
+size_t render_scratch_bytes(uint64_t paths, uint32_t depth);
 cudaError_t launch_accum_clear(float* accum, uint32_t w, uint32_t h, void* stream);
 cudaError_t launch_resolve(const float* accum, uint32_t w, uint32_t h, uint32_t spp, float* out, void* stream);
 int device_sm_count();

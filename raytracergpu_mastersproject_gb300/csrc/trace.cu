@@ -11,6 +11,7 @@
 //                 refill as soon as `refill` lanes are idle (the default).
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstdlib>
 #include <type_traits>
 #include <mutex>
@@ -102,7 +103,12 @@ __global__ void __launch_bounds__(THREADS, MINB)
 // ray by exactly one step -- one inner node, or one leaf -- and lanes whose ray
 // finished take new rays as soon as `refill` of them are idle.  The heavy
 // inner-node step then runs with nearly all lanes active; leaves are rare.
-template <bool ANY, int STACK, int THREADS, int MINB, bool STATS>
+//
+// RAW (the path tracer's queries): n == 0xFFFFFFFF reads the ray count from
+// counter[2], written by the kernel that produced the rays; each hit is the
+// traversal's own result -- the leaf-style ref of the closest primitive (0:
+// none, kRawOverflow: stack overflow) and t -- so that shading needs no id map.
+template <bool ANY, int STACK, int THREADS, int MINB, bool STATS, bool RAW = false>
 __global__ void __launch_bounds__(THREADS, MINB)
     k_trace_step(DeviceScene S, const float4* __restrict__ rays, uint32_t n, uint2* __restrict__ hits,
                  uint32_t* __restrict__ counter, int refill, unsigned long long* __restrict__ stats,
@@ -110,6 +116,7 @@ __global__ void __launch_bounds__(THREADS, MINB)
   uint2 stack[STACK];
   dev::Trav s;
   const uint32_t lane = threadIdx.x & 31u;
+  if (RAW && n == 0xFFFFFFFFu) n = *reinterpret_cast<volatile uint32_t*>(counter + 2);
   uint32_t ray = 0xFFFFFFFFu;
   bool exhausted = false;
   unsigned long long vis = 0, tests = 0;
@@ -146,7 +153,10 @@ __global__ void __launch_bounds__(THREADS, MINB)
     }
     if (done || s.node == kSentinel) {
       uint2 h;
-      if (s.sp < 0 || s.best == dev::kNoBest) {
+      if (RAW) {
+        h.x = s.sp < 0 ? kRawOverflow : s.best;
+        h.y = __float_as_uint(s.tclose);
+      } else if (s.sp < 0 || s.best == dev::kNoBest) {
         h.x = RT_NO_HIT;
         h.y = __float_as_uint(__int_as_float(0x7f800000));
       } else if (s.best & kSphereBit) {
@@ -296,6 +306,27 @@ int device_sm_count() {
 cudaError_t launch_trace(const DeviceScene& s, const RtRay* rays, uint32_t n, RtHit* hits, uint32_t flags,
                          uint32_t* counter, void* stream, const uint32_t* order) {
   return launch_trace_tuned(s, rays, n, hits, flags, counter, stream, default_tuning(), nullptr, order);
+}
+
+cudaError_t launch_trace_raw(const DeviceScene& S, const float4* rays, uint32_t n, uint2* hits, uint32_t* counter,
+                             unsigned long long* stats, cudaStream_t st) {
+  constexpr int T = 128, M = 12;
+  const bool big = S.stack_need > 64u;
+  const int k = (big ? 1 : 0) | (stats ? 2 : 0);
+  static int bps[4] = {-1, -1, -1, -1};
+  TraceKernel kern = big ? (stats ? k_trace_step<false, 192, T, M, true, true> : k_trace_step<false, 192, T, M, false, true>)
+                         : (stats ? k_trace_step<false, 64, T, M, true, true> : k_trace_step<false, 64, T, M, false, true>);
+  if (bps[k] < 0) {
+    int b = 0;
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, kern, T, 0);
+    if (e != cudaSuccess) return e;
+    bps[k] = b < 1 ? 1 : b;
+  }
+  uint64_t blocks = (uint64_t)device_sm_count() * (uint64_t)bps[k];
+  if (n != 0xFFFFFFFFu) blocks = std::min<uint64_t>(blocks, ((uint64_t)n + T - 1) / T);
+  if (blocks == 0) blocks = 1;
+  kern<<<(uint32_t)blocks, T, 0, st>>>(S, rays, n, hits, counter, default_tuning().refill, stats, nullptr);
+  return cudaGetLastError();
 }
 
 // ---- allocation-free ray queries (rt_trace_noalloc) ----

@@ -173,3 +173,86 @@ def test_depth_zero_advances_rng_only(rt, cuda):
     px = a.reshape(-1, 4)
     assert np.all(px[:, :3] == 0.0)
     assert np.all(px[:, 3] != 1.0)
+
+
+def test_render_count_matches_render(rt, cuda):
+    """rt_render_count renders the same frame as rt_render and counts one
+    closest-hit query per traced bounce; both kernels count the same queries."""
+    tris, mats = rt.gen_spheres_scene(2, 64, 3, 0.05)
+    ubo = rt.make_ubo((0.0, 3.0, 28.0), (0.0, 0.0, 0.0), fov=40.0, depth=8, random_state=2,
+                      num_triangles=len(tris), num_materials=len(mats))
+    w, h, spp = 96, 54, 2
+    kw = {"shade_mode": rt.SHADE_EXTENDED, "background": (0.6, 0.7, 1.0)}
+    counts = {}
+    for width in (2, 4):
+        with rt.Scene(tris, materials=mats, node_width=width) as sc:
+            a = gpu_render(rt, cuda, sc, ubo, w, h, spp, **kw)
+            for every in (False, True):
+                acc = cuda.empty(w * h * 4, dtype=cuda.float32, device="cuda")
+                rt.accum_clear(acc, w, h)
+                counts[width, every] = sc.render_count(ubo, acc, w, h, spp, trace_every_primary=every, **kw)
+                cuda.cuda.synchronize()
+                assert np.array_equal(acc.cpu().numpy(), a)
+    q2, n2, p2 = counts[2, True]
+    q4, n4, p4 = counts[4, True]
+    assert counts[2, False] == counts[2, True]  # the per-pixel kernel traces every primary ray
+    assert q2 == q4
+    assert w * h * spp <= q4 <= w * h * spp * 8
+    assert n4 > 0 and p4 > 0 and n2 > n4
+    # sharing the first hit saves exactly one query per pixel and later sample
+    assert counts[4, False][0] == q4 - w * h * (spp - 1)
+
+
+def test_shared_first_hit_is_exact(rt, cuda):
+    """Samples 1.. of a pixel reuse sample 0's first hit (the camera has no
+    jitter); the frame equals the one that traces every primary ray."""
+    tris, mats = rt.gen_spheres_scene(5, 16, 3, 0.05)
+    ubo = rt.make_ubo((0.0, 3.0, 28.0), (0.0, 0.0, 0.0), fov=40.0, depth=6, random_state=11,
+                      num_triangles=len(tris), num_materials=len(mats))
+    w, h = 120, 68
+    for kw in ({}, {"shade_mode": rt.SHADE_EXTENDED, "background": (0.6, 0.7, 1.0)}):
+        with rt.Scene(tris, materials=mats, node_width=4) as sc:
+            a = gpu_render(rt, cuda, sc, ubo, w, h, 5, **kw)
+            b = gpu_render(rt, cuda, sc, ubo, w, h, 5, trace_every_primary=True, **kw)
+            c = gpu_render(rt, cuda, sc, ubo, w, h, 1, calls=5, **kw)
+        assert np.array_equal(a, b)
+        assert np.array_equal(a, c)
+
+
+@pytest.mark.parametrize("paths", ["777", "4"])
+def test_wavefront_passes_match(rt, cuda, tmp_path, paths):
+    """The wavefront renderer splits a frame into passes when its paths do not
+    fit the scratch: room for 777 paths gives chunks of 86 pixels x 9 samples;
+    room for 4 gives one pixel at a time in sample passes of 4, 4 and 1 (the
+    alpha carry links the passes).  The frame is unchanged either way."""
+    import os
+    import subprocess
+    import sys
+
+    tris, mats = lit_scene(rt)
+    ubo = rt.make_ubo((0.0, 0.5, 4.0), (0.0, 0.0, 0.0), fov=60.0, depth=5, random_state=77)
+    w, h = 53, 29
+    with rt.Scene(tris, materials=mats, node_width=4) as sc:
+        a = gpu_render(rt, cuda, sc, ubo, w, h, 9, shade_mode=rt.SHADE_EXTENDED, background=(0.3, 0.4, 0.5))
+    np.save(tmp_path / "a.npy", a)
+    code = f"""
+import numpy as np, torch, sys
+sys.path.insert(0, {repr(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))})
+import raytracergpu_mastersproject_gb300 as rt
+sph = rt.gen_icosphere(3, (0.0, 0.0, 0.0), 1.0, 0)
+tris = np.concatenate([sph, rt.gen_config1()[0][-2:]])
+mats = np.zeros(2, rt.MATERIAL_DTYPE)
+mats[0]["albedo"][:3] = (0.73, 0.33, 0.25); mats[0]["materialType"] = rt.MAT_DIFFUSE
+mats[1]["albedo"][:3] = (3.0, 3.0, 3.0); mats[1]["materialType"] = rt.MAT_LIGHT
+ubo = rt.make_ubo((0.0, 0.5, 4.0), (0.0, 0.0, 0.0), fov=60.0, depth=5, random_state=77)
+acc = torch.empty({w} * {h} * 4, dtype=torch.float32, device="cuda")
+rt.accum_clear(acc, {w}, {h})
+with rt.Scene(tris, materials=mats, node_width=4) as sc:
+    sc.render(ubo, acc, {w}, {h}, 9, shade_mode=rt.SHADE_EXTENDED, background=(0.3, 0.4, 0.5))
+torch.cuda.synchronize()
+np.save({repr(str(tmp_path / "b.npy"))}, acc.cpu().numpy())
+"""
+    env = dict(os.environ, RT_RENDER_WAVE_PATHS=paths)
+    p = subprocess.run([sys.executable, "-c", code], env=env, capture_output=True, text=True, timeout=300)
+    assert p.returncode == 0, p.stderr
+    assert np.array_equal(np.load(tmp_path / "b.npy"), a)
