@@ -393,10 +393,16 @@ __global__ void __launch_bounds__(THREADS, MINB)
 // sample order at the end (k_wave_accum), so the accumulator is the same as
 // with one lane running the pixel's samples back to back.
 //
-// Scratch per path: state (color.xyz, rng | gatt.xyz, -) 32 B, two ray
-// buffers 2 x 32 B, two path lists 2 x 4 B, hits 8 B.
+// Path p of a pass over npix pixels x ns samples is sample p % ns of pixel
+// p / ns: a pixel's samples start from the same hit point, and kept adjacent
+// they keep their next rays in the same warps.  The starting RNG states are
+// stored sample-major (rng0[k * npix + q]) so that k_wave_seed's stores are
+// coalesced.  Scratch per path: state (color.xyz, rng | gatt.xyz, -) 32 B,
+// the starting RNG state 4 B, two ray buffers 2 x 32 B, two path lists
+// 2 x 4 B, hits 8 B.
 struct WaveBufs {
   float4* state;  // 2 float4 per path
+  uint32_t* rng0;
   float4* rays[2];
   uint32_t* list[2];
   uint2* hits;
@@ -404,7 +410,7 @@ struct WaveBufs {
 };
 
 __global__ void k_wave_seed(Cam cam, uint32_t random_state, float4* __restrict__ accum, uint32_t Wd, uint32_t pix0,
-                            uint32_t npix, uint32_t ns, uint32_t per_path, float4* __restrict__ state,
+                            uint32_t npix, uint32_t ns, uint32_t per_path, uint32_t* __restrict__ rng0,
                             float4* __restrict__ rays) {
   for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < npix; q += gridDim.x * blockDim.x) {
     const uint32_t pix = pix0 + q;
@@ -414,9 +420,7 @@ __global__ void k_wave_seed(Cam cam, uint32_t random_state, float4* __restrict__
       uint32_t rng = (600u * x + y) * (random_state + 1u);  // random.glsl:9
       rng += __float2uint_rz(px.w * 4294967294.0f);         // raytraceBVH.comp:350, saturating
       px.w = rng_next(rng);                                 // :352 (:351 is a no-op)
-      const size_t p = (size_t)q * ns + k;
-      state[2 * p] = make_float4(0.0f, 0.0f, 0.0f, __uint_as_float(rng));
-      state[2 * p + 1] = make_float4(1.0f, 1.0f, 1.0f, 0.0f);
+      rng0[(size_t)k * npix + q] = rng;
     }
     accum[pix] = px;  // the carry after these samples; the colours are added by k_wave_accum
     const f3 pos = mk(cam.v[0], cam.v[1], cam.v[2]);
@@ -438,18 +442,20 @@ __global__ void k_wave_seed(Cam cam, uint32_t random_state, float4* __restrict__
   }
 }
 
-// Shades level `level`: n0 rays at level 0 (path p's ray is rays[p] or, when
-// the pixel's first hit is shared, rays[p / ns]); later levels take the count
-// from the level's counter block and path ids from `list`.
+// Shades level `level`: n0 = npix * ns paths at level 0 (path p's ray is
+// rays[p] or, when the pixel's first hit is shared, rays[p / ns]; colour 0,
+// throughput 1, RNG from rng0); later levels take the count from the level's
+// counter block and path ids from `list`.
 template <bool STATS>
-__global__ void k_wave_shade(DeviceScene S, uint32_t level, uint32_t depth, uint32_t n0, uint32_t ns, uint32_t per_path,
-                             uint32_t mode, float bgx, float bgy, float bgz, float4* __restrict__ state,
+__global__ void k_wave_shade(DeviceScene S, uint32_t level, uint32_t depth, uint32_t n0, uint32_t npix, uint32_t ns,
+                             uint32_t per_path, uint32_t mode, float bgx, float bgy, float bgz,
+                             float4* __restrict__ state, const uint32_t* __restrict__ rng0,
                              const float4* __restrict__ rays, const uint32_t* __restrict__ list,
                              const uint2* __restrict__ hits, float4* __restrict__ next_rays,
                              uint32_t* __restrict__ next_list, uint32_t* __restrict__ cnt,
                              uint32_t* __restrict__ status_word, unsigned long long* __restrict__ stats) {
   const uint32_t n = level == 0 ? n0 : *reinterpret_cast<volatile uint32_t*>(cnt + 4u * level + 2u);
-  if (STATS && level == 0 && blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&stats[0], (unsigned long long)(per_path ? n0 : n0 / ns));
+  if (STATS && level == 0 && blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&stats[0], (unsigned long long)(per_path ? n0 : npix));
   if (STATS && level > 0 && blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&stats[0], (unsigned long long)n);
   const bool extended = (mode & kRenderExtended) != 0u;
   const f3 bg = mk(bgx, bgy, bgz);
@@ -469,9 +475,16 @@ __global__ void k_wave_shade(DeviceScene S, uint32_t level, uint32_t depth, uint
       s.best = h.x == kRawOverflow ? 0u : h.x;
       s.sp = h.x == kRawOverflow ? -1 : 0;
       s.tclose = __uint_as_float(h.y);
-      float4 a = state[2 * (size_t)p], g = state[2 * (size_t)p + 1];
-      f3 color = mk(a.x, a.y, a.z), gatt = mk(g.x, g.y, g.z);
-      uint32_t rng = __float_as_uint(a.w);
+      f3 color = mk(0.0f, 0.0f, 0.0f), gatt = mk(1.0f, 1.0f, 1.0f);
+      uint32_t rng;
+      if (level == 0) {
+        rng = rng0[(size_t)(p % ns) * npix + p / ns];
+      } else {
+        const float4 a = state[2 * (size_t)p], g = state[2 * (size_t)p + 1];
+        color = mk(a.x, a.y, a.z);
+        gatt = mk(g.x, g.y, g.z);
+        rng = __float_as_uint(a.w);
+      }
       co = mk(o.x, o.y, o.z);
       cd = mk(d.x, d.y, d.z);
       more = bounce(S, s, co, cd, color, gatt, rng, extended, bg, status) && level + 1u < depth;
@@ -510,7 +523,7 @@ __global__ void k_wave_accum(float4* __restrict__ accum, uint32_t pix0, uint32_t
   }
 }
 
-constexpr size_t kWaveBytesPerPath = 32 + 64 + 8 + 8;
+constexpr size_t kWaveBytesPerPath = 32 + 4 + 64 + 8 + 8;
 // Two launches per level: deeper paths go to k_render_step instead.
 constexpr uint32_t kWaveMaxDepth = 64;
 
@@ -521,6 +534,8 @@ WaveBufs wave_bufs(void* scratch, uint64_t paths, uint32_t depth) {
   size_t off = 0;
   w.state = reinterpret_cast<float4*>(b + off);
   off += up(paths * 32);
+  w.rng0 = reinterpret_cast<uint32_t*>(b + off);
+  off += up(paths * 4);
   w.rays[0] = reinterpret_cast<float4*>(b + off);
   off += up(paths * 32);
   w.rays[1] = reinterpret_cast<float4*>(b + off);
@@ -557,16 +572,16 @@ cudaError_t launch_render_wave(const DeviceScene& S, const Cam& cam, uint32_t de
       const uint32_t np = q * ns;
       if ((e = cudaMemsetAsync(B.cnt, 0, 16 * ((size_t)depth + 1), st)) != cudaSuccess) return e;
       const uint32_t gb = std::min<uint32_t>(sms * 8, (q + 255) / 256);
-      k_wave_seed<<<gb, 256, 0, st>>>(cam, rs, accum, Wd, pix0, q, ns, per_path, B.state, B.rays[0]);
+      k_wave_seed<<<gb, 256, 0, st>>>(cam, rs, accum, Wd, pix0, q, ns, per_path, B.rng0, B.rays[0]);
       for (uint32_t l = 0; l < depth; ++l) {
         const float4* r = B.rays[l & 1u];
         if ((e = launch_trace_raw(S, r, l == 0 ? (per_path ? np : q) : 0xFFFFFFFFu, B.hits, B.cnt + 4u * l,
                                   trace_stats, st)) != cudaSuccess)
           return e;
         const uint32_t gs = l == 0 ? std::min<uint32_t>(sms * 8, (np + 255) / 256) : sms * 8;
-        k_wave_shade<STATS><<<gs, 256, 0, st>>>(S, l, depth, np, ns, per_path, mode, bg[0], bg[1], bg[2], B.state, r,
-                                                B.list[l & 1u], B.hits, B.rays[(l + 1u) & 1u], B.list[(l + 1u) & 1u],
-                                                B.cnt, counter + 1, stats);
+        k_wave_shade<STATS><<<gs, 256, 0, st>>>(S, l, depth, np, q, ns, per_path, mode, bg[0], bg[1], bg[2], B.state,
+                                                B.rng0, r, B.list[l & 1u], B.hits, B.rays[(l + 1u) & 1u],
+                                                B.list[(l + 1u) & 1u], B.cnt, counter + 1, stats);
       }
       k_wave_accum<<<gb, 256, 0, st>>>(accum, pix0, q, ns, B.state);
       if ((e = cudaGetLastError()) != cudaSuccess) return e;
@@ -701,7 +716,7 @@ bool render_uses_scratch(const DeviceScene& s, uint32_t depth) {
 }
 
 size_t render_scratch_bytes(uint64_t paths, uint32_t depth) {
-  return (size_t)paths * kWaveBytesPerPath + 7 * 256 + 16 * ((size_t)depth + 1);
+  return (size_t)paths * kWaveBytesPerPath + 8 * 256 + 16 * ((size_t)depth + 1);
 }
 
 cudaError_t launch_accum_clear(float* accum, uint32_t w, uint32_t h, void* stream) {
