@@ -39,11 +39,11 @@ sys.path.insert(0, str(ROOT))
 
 METRIC = "closest-hit Grays/s batched vs plain per-call launch; served p50/p99 latency"
 UNIT = "Grays/s"
+L2_BYTES = 129 * 10**6
 N_TRIS = 4_194_304
 N_RAYS = 16_777_216
 SEED = 3
 CPU_SAMPLE = 2_097_152
-COUNT_SAMPLE = 65_536
 # DRAM bytes per ray of k_trace_step on the full config-3 BVH, from the ncu
 # capture summarised in profiles/k_trace_step_config3.md (2,097,152 rays,
 # dram__bytes_read.sum + dram__bytes_write.sum = 2.502 GB).
@@ -78,6 +78,16 @@ def dist_env():
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
     return ws, rank, local
+
+
+def l2_note(n_rays: int, info) -> str:
+    """Whether the timed inputs exceed the 129 MB L2 (no flush between steps then)."""
+    ray_b = n_rays * 32
+    scene_b = info.device_nodes * 64 + info.num_triangles * 64
+    big = ray_b + n_rays * 8 > L2_BYTES and scene_b > L2_BYTES
+    return (f"rays {ray_b / 2**20:.0f} MiB + hits {n_rays * 8 / 2**20:.0f} MiB, nodes+triangles "
+            f"{scene_b / 2**20:.0f} MiB; " + ("both larger than L2, no flush" if big else
+                                               "not both larger than L2 (a parity/shape run, not a bench value)"))
 
 
 def reduce_max(x: float, dist=None, device="cpu") -> float:
@@ -185,7 +195,7 @@ def cpu_leg(tris, nodes, rays, sample: int) -> tuple[dict, dict]:
     t0 = time.perf_counter()
     ref_hits, st = orc.trace(S, sub, canonical=False, nthreads=cores)
     dt = time.perf_counter() - t0
-    cnt = np.ascontiguousarray(rays[:COUNT_SAMPLE])
+    cnt = sub
     t1 = time.perf_counter()
     can_hits, cst = orc.trace(S, cnt, canonical=True, nthreads=cores)
     dt_can = time.perf_counter() - t1
@@ -553,7 +563,7 @@ def run_ours(args):
                        "triangles": args.tris, "rays": n, "bvh": "host LBVH, sorted leaves",
                        "leaf_size": info.leaf_size, "node_width": info.node_width,
                        "device_nodes": info.device_nodes, "bvh_depth": info.depth, "stack_need": info.stack_need,
-                       "l2": "inputs larger than L2 (rays 512 MiB, nodes+triangles 512 MiB); no flush",
+                       "l2": l2_note(n, info),
                        "ray_order": "origin-bucketed inside the step (RT_TRACE_SORT)" if sort else "as given",
                        "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU"},
             "roofline": roof, "cpu_baseline": cpu_base, "e2e": e2e, "clocks": clk,
