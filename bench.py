@@ -47,7 +47,7 @@ CPU_SAMPLE = 2_097_152
 # DRAM bytes per ray of k_trace_step on the full config-3 BVH, from the ncu
 # capture summarised in profiles/k_trace_step_config3.md (2,097,152 rays,
 # dram__bytes_read.sum + dram__bytes_write.sum = 2.502 GB).
-DRAM_BYTES_PER_RAY = 2.502e9 / 2_097_152
+DRAM_BYTES_PER_RAY = (1.453224e9 + 61.520384e6) / 2_097_152  # ncu, 2 Mi-ray launch on the config-3 tree
 
 
 def parse():
@@ -255,7 +255,7 @@ def run_batched(torch, rt) -> dict:
     batched()
     torch.cuda.synchronize()
     same = all(torch.equal(a, b) for a, b in zip(dh_plain, dh_batch))
-    thr, minb = rt.describe_pool_variant(variant)
+    thr, minb, ring = rt.describe_pool_variant(variant)
     out = {"workload": "config 4: 256 triangle soups, counts log-uniform in [1K, 256K], each with a ray batch "
                        "log-uniform in [4K, 1M] rays, closest-hit",
            "triangles": nt, "rays": nr, "unit": UNIT,
@@ -263,7 +263,8 @@ def run_batched(torch, rt) -> dict:
                      "path": "one rt_trace per scene"},
            "batched": {"value": nr / ms_batch / 1e6, "ms": ms_batch, "launches": 1, "cuda_graph": True,
                        "untuned_ms": ms_untuned,
-                       "autotuned": {"threads_per_block": thr, "min_blocks_per_sm": minb, "refill": refill}},
+                       "autotuned": {"threads_per_block": thr, "min_blocks_per_sm": minb,
+                                     "stack_entries_in_shared_memory": ring, "refill": refill}},
            "speedup": ms_plain / ms_batch, "identical_hits": bool(same)}
     pool.close()
     for sc in scenes:

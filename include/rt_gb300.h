@@ -320,7 +320,11 @@ rt_status rt_pool_trace(rt_pool* pool, const RtJob* jobs, uint32_t num_jobs, uin
  * later rt_pool_trace calls.  Synchronous. */
 rt_status rt_pool_autotune(rt_pool* pool, const RtJob* jobs, uint32_t num_jobs, uint32_t flags, void* stream,
                            uint32_t repeats);
-rt_status rt_pool_describe_variant(uint32_t variant, uint32_t* threads, uint32_t* min_blocks);
+/* Launch shape of a variant: threads per block, minimum resident blocks per
+ * SM (the register cap), and the traversal-stack entries kept in shared
+ * memory per lane (0: all in local memory).  stack_ring may be NULL. */
+rt_status rt_pool_describe_variant(uint32_t variant, uint32_t* threads, uint32_t* min_blocks,
+                                   uint32_t* stack_ring);
 
 /* ---------------------------------------------------------------- serving */
 /* A request loop over a scene pool (no counterpart in the reference): keeps

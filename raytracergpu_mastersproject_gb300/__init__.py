@@ -157,7 +157,7 @@ SIGNATURES = {
     "rt_pool_get_info": (_I, [_P, C.POINTER(PoolInfo)]),
     "rt_pool_trace": (_I, [_P, C.POINTER(Job), _U32, _U32, _P]),
     "rt_pool_autotune": (_I, [_P, C.POINTER(Job), _U32, _U32, _P, _U32]),
-    "rt_pool_describe_variant": (_I, [_U32, C.POINTER(_U32), C.POINTER(_U32)]),
+    "rt_pool_describe_variant": (_I, [_U32, C.POINTER(_U32), C.POINTER(_U32), C.POINTER(_U32)]),
     "rt_server_create": (_I, [C.POINTER(ServerOptions), C.POINTER(C.c_void_p)]),
     "rt_server_destroy": (_I, [_P]),
     "rt_server_upload": (_I, [_P, C.POINTER(_SceneDesc), C.POINTER(_U64)]),
@@ -539,10 +539,11 @@ class Server:
         self.close()
 
 
-def describe_pool_variant(v: int) -> tuple[int, int]:
-    t, m = C.c_uint32(), C.c_uint32()
-    _check(lib().rt_pool_describe_variant(v, C.byref(t), C.byref(m)), "rt_pool_describe_variant")
-    return t.value, m.value
+def describe_pool_variant(v: int) -> tuple[int, int, int]:
+    """-> (threads per block, minimum blocks per SM, stack entries per lane in shared memory)."""
+    t, m, r = C.c_uint32(), C.c_uint32(), C.c_uint32()
+    _check(lib().rt_pool_describe_variant(v, C.byref(t), C.byref(m), C.byref(r)), "rt_pool_describe_variant")
+    return t.value, m.value, r.value
 
 
 def build_bvh(triangles, spheres=None, models=None, bvh_mode: int = BVH_SORTED) -> np.ndarray:

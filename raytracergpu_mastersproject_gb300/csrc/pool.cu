@@ -14,6 +14,8 @@
 // device copy and a captured CUDA graph (table upload, queue reset, kernel).
 #include <cuda_runtime.h>
 
+#include <type_traits>
+
 #include <chrono>
 #include <cstring>
 #include <map>
@@ -63,10 +65,23 @@ __device__ __forceinline__ uint32_t find_job(const DJob* __restrict__ jobs, uint
 
 // k_trace_step over a job table (see trace.cu): each lane keeps (job, local
 // ray index) and its job's root; hits go to the job's own hit array.
-template <bool ANY, int STACK, int THREADS, int MINB>
+// RING > 0: the top RING stack entries of each lane in shared memory (see
+// dev::RingStack).
+template <bool ANY, int STACK, int THREADS, int MINB, int RING>
 __global__ void __launch_bounds__(THREADS, MINB)
     k_pool_step(DeviceScene S, const DJob* __restrict__ table, uint32_t* __restrict__ counter, int refill) {
   uint2 stack[STACK];
+  using Stk = typename std::conditional<(RING > 0), dev::RingStack<(RING > 0 ? RING : 1), THREADS>,
+                                        dev::LocalStack>::type;
+  Stk stk;
+  if constexpr (RING > 0) {
+    __shared__ uint2 ring[RING * THREADS];
+    stk.ring = ring + threadIdx.x;
+    stk.spill = stack;
+    stk.lo = 0;
+  } else {
+    stk.a = stack;
+  }
   dev::Trav s;
   const uint32_t lane = threadIdx.x & 31u;
   const uint32_t num_jobs = __ldg(reinterpret_cast<const uint32_t*>(table));
@@ -90,6 +105,7 @@ __global__ void __launch_bounds__(THREADS, MINB)
           local = g - __ldg(&jobs[job].start);
           const float4* rays = jobs[job].rays;
           dev::trav_init_ray(s, __ldg(&rays[2u * local]), __ldg(&rays[2u * local + 1u]), __ldg(&jobs[job].root));
+          stk.reset();
           if (s.leaf != 0u) {
             s.node = s.leaf;
             s.leaf = 0u;
@@ -100,12 +116,12 @@ __global__ void __launch_bounds__(THREADS, MINB)
     if (local == 0xFFFFFFFFu) continue;
     bool done = false;
     if (dev::is_inner(s.node)) {
-      if (!dev::visit_wide<STACK>(S, s, stack)) done = true;
+      if (!dev::visit_wide_stk<STACK>(S, s, stk)) done = true;
     } else if (dev::is_leaf(s.node)) {
       if (dev::leaf_visit<ANY>(S, s, s.node))
         done = true;
       else
-        s.node = dev::pop_wide(s, stack);
+        s.node = stk.pop(s);
     }
     if (done || s.node == kSentinel) {
       uint2 h;
@@ -125,21 +141,23 @@ __global__ void __launch_bounds__(THREADS, MINB)
 using PoolKernel = void (*)(DeviceScene, const DJob*, uint32_t*, int);
 
 struct PoolVariant {
-  int threads, minb;
+  int threads, minb, ring;
   PoolKernel k[2][2];  // [any][stack 192]
   int bps[2][2];
 };
 
-template <int T, int M>
+template <int T, int M, int R>
 PoolVariant make_pool_variant() {
-  PoolVariant v{T, M, {{k_pool_step<false, 64, T, M>, k_pool_step<false, 192, T, M>},
-                       {k_pool_step<true, 64, T, M>, k_pool_step<true, 192, T, M>}},
+  PoolVariant v{T, M, R, {{k_pool_step<false, 64, T, M, R>, k_pool_step<false, 192, T, M, R>},
+                          {k_pool_step<true, 64, T, M, R>, k_pool_step<true, 192, T, M, R>}},
                 {{-1, -1}, {-1, -1}}};
   return v;
 }
 
-PoolVariant g_pool_variants[] = {make_pool_variant<128, 12>(), make_pool_variant<128, 10>(),
-                                 make_pool_variant<128, 1>(), make_pool_variant<256, 6>()};
+// Variant 0 is the default before rt_pool_autotune.
+PoolVariant g_pool_variants[] = {make_pool_variant<128, 10, 16>(), make_pool_variant<256, 5, 16>(),
+                                 make_pool_variant<128, 12, 0>(), make_pool_variant<128, 10, 0>(),
+                                 make_pool_variant<256, 6, 0>()};
 constexpr int kNumPoolVariants = sizeof(g_pool_variants) / sizeof(g_pool_variants[0]);
 
 // First-fit range allocator over [0, capacity) with coalescing frees.
@@ -682,10 +700,11 @@ rt_status rt_pool_autotune(rt_pool* P, const RtJob* jobs, uint32_t num_jobs, uin
   return RT_OK;
 }
 
-rt_status rt_pool_describe_variant(uint32_t v, uint32_t* threads, uint32_t* min_blocks) {
+rt_status rt_pool_describe_variant(uint32_t v, uint32_t* threads, uint32_t* min_blocks, uint32_t* stack_ring) {
   if (v >= (uint32_t)kNumPoolVariants || !threads || !min_blocks) return RT_EINVAL;
   *threads = (uint32_t)g_pool_variants[v].threads;
   *min_blocks = (uint32_t)g_pool_variants[v].minb;
+  if (stack_ring) *stack_ring = (uint32_t)g_pool_variants[v].ring;
   return RT_OK;
 }
 

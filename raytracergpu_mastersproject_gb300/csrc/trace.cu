@@ -8,7 +8,8 @@
 //                 and 4-wide trees); idle lanes are refilled when fewer than
 //                 `refill` lanes still traverse.
 //   k_trace_step  4-wide trees: one traversal step per lane per iteration and
-//                 refill as soon as `refill` lanes are idle (the default).
+//                 refill as soon as `refill` lanes are idle (the default, with
+//                 the top 16 stack entries of each lane in shared memory).
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -108,12 +109,26 @@ __global__ void __launch_bounds__(THREADS, MINB)
 // counter[2], written by the kernel that produced the rays; each hit is the
 // traversal's own result -- the leaf-style ref of the closest primitive (0:
 // none, kRawOverflow: stack overflow) and t -- so that shading needs no id map.
-template <bool ANY, int STACK, int THREADS, int MINB, bool STATS, bool RAW = false>
+//
+// RING > 0 keeps the top RING stack entries of each lane in shared memory
+// (RING * THREADS * 8 bytes per block), the rest in local memory.
+template <bool ANY, int STACK, int THREADS, int MINB, bool STATS, bool RAW = false, int RING = 0>
 __global__ void __launch_bounds__(THREADS, MINB)
     k_trace_step(DeviceScene S, const float4* __restrict__ rays, uint32_t n, uint2* __restrict__ hits,
                  uint32_t* __restrict__ counter, int refill, unsigned long long* __restrict__ stats,
             const uint32_t* __restrict__ order) {
   uint2 stack[STACK];
+  using Stk = typename std::conditional<(RING > 0), dev::RingStack<(RING > 0 ? RING : 1), THREADS>,
+                                        dev::LocalStack>::type;
+  Stk stk;
+  if constexpr (RING > 0) {
+    __shared__ uint2 ring[RING * THREADS];
+    stk.ring = ring + threadIdx.x;
+    stk.spill = stack;
+    stk.lo = 0;
+  } else {
+    stk.a = stack;
+  }
   dev::Trav s;
   const uint32_t lane = threadIdx.x & 31u;
   if (RAW && n == 0xFFFFFFFFu) n = *reinterpret_cast<volatile uint32_t*>(counter + 2);
@@ -134,6 +149,7 @@ __global__ void __launch_bounds__(THREADS, MINB)
         if (id < n) {
           ray = order ? __ldg(&order[id]) : id;
           dev::trav_init_ray(s, __ldg(&rays[2u * ray]), __ldg(&rays[2u * ray + 1u]), S.root);
+          stk.reset();
           if (s.leaf != 0u) {  // the whole tree is one leaf
             s.node = s.leaf;
             s.leaf = 0u;
@@ -144,12 +160,12 @@ __global__ void __launch_bounds__(THREADS, MINB)
     if (ray == 0xFFFFFFFFu) continue;
     bool done = false;
     if (dev::is_inner(s.node)) {
-      if (!dev::visit_wide<STACK>(S, s, stack)) done = true;
+      if (!dev::visit_wide_stk<STACK>(S, s, stk)) done = true;
     } else if (dev::is_leaf(s.node)) {
       if (dev::leaf_visit<ANY>(S, s, s.node))
         done = true;
       else
-        s.node = dev::pop_wide(s, stack);
+        s.node = stk.pop(s);
     }
     if (done || s.node == kSentinel) {
       uint2 h;
@@ -209,23 +225,23 @@ void fill_variant(Variant& v) {
   v.k[ST][1][1][1] = k_trace<true, 192, T, M, 4, ST>;
 }
 
-template <int T, int M, bool ST>
+template <int T, int M, bool ST, int RING>
 void fill_step_variant(Variant& v) {
   fill_variant<T, M, ST>(v);  // binary trees keep the while-while loop
-  v.k[ST][1][0][0] = k_trace_step<false, 64, T, M, ST>;
-  v.k[ST][1][0][1] = k_trace_step<false, 192, T, M, ST>;
-  v.k[ST][1][1][0] = k_trace_step<true, 64, T, M, ST>;
-  v.k[ST][1][1][1] = k_trace_step<true, 192, T, M, ST>;
+  v.k[ST][1][0][0] = k_trace_step<false, 64, T, M, ST, false, RING>;
+  v.k[ST][1][0][1] = k_trace_step<false, 192, T, M, ST, false, RING>;
+  v.k[ST][1][1][0] = k_trace_step<true, 64, T, M, ST, false, RING>;
+  v.k[ST][1][1][1] = k_trace_step<true, 192, T, M, ST, false, RING>;
 }
 
-template <int T, int M, bool STEP>
+template <int T, int M, bool STEP, int RING = 0>
 Variant make_variant() {
   Variant v;
   v.threads = T;
   v.minb = M;
   if constexpr (STEP) {
-    fill_step_variant<T, M, false>(v);
-    fill_step_variant<T, M, true>(v);
+    fill_step_variant<T, M, false, RING>(v);
+    fill_step_variant<T, M, true, RING>(v);
   } else {
     fill_variant<T, M, false>(v);
     fill_variant<T, M, true>(v);
@@ -238,7 +254,8 @@ Variant make_variant() {
 }
 
 Variant g_variants[] = {make_variant<128, 12, false>(), make_variant<128, 10, false>(), make_variant<128, 1, false>(),
-                        make_variant<128, 12, true>(),  make_variant<128, 10, true>(),  make_variant<128, 1, true>()};
+                        make_variant<128, 12, true>(),  make_variant<128, 10, true>(),  make_variant<128, 1, true>(),
+                        make_variant<128, 10, true, 16>(), make_variant<256, 5, true, 16>()};
 constexpr int kNumVariants = sizeof(g_variants) / sizeof(g_variants[0]);
 
 int env_int(const char* name, int dflt) {
@@ -251,7 +268,7 @@ int env_int(const char* name, int dflt) {
 TraceTuning default_tuning() {
   static TraceTuning t = [] {
     TraceTuning d;
-    d.variant = env_int("RT_TRACE_VARIANT", 3);
+    d.variant = env_int("RT_TRACE_VARIANT", 6);
     d.refill = env_int("RT_TRACE_REFILL", 4);
     d.grid_scale = env_int("RT_TRACE_GRID_PCT", 100);
     return d;
@@ -310,12 +327,14 @@ cudaError_t launch_trace(const DeviceScene& s, const RtRay* rays, uint32_t n, Rt
 
 cudaError_t launch_trace_raw(const DeviceScene& S, const float4* rays, uint32_t n, uint2* hits, uint32_t* counter,
                              unsigned long long* stats, cudaStream_t st) {
-  constexpr int T = 128, M = 12;
+  constexpr int T = 128, M = 10, R = 16;  // the default ray-query shape
   const bool big = S.stack_need > 64u;
   const int k = (big ? 1 : 0) | (stats ? 2 : 0);
   static int bps[4] = {-1, -1, -1, -1};
-  TraceKernel kern = big ? (stats ? k_trace_step<false, 192, T, M, true, true> : k_trace_step<false, 192, T, M, false, true>)
-                         : (stats ? k_trace_step<false, 64, T, M, true, true> : k_trace_step<false, 64, T, M, false, true>);
+  TraceKernel kern = big ? (stats ? k_trace_step<false, 192, T, M, true, true, R>
+                                  : k_trace_step<false, 192, T, M, false, true, R>)
+                         : (stats ? k_trace_step<false, 64, T, M, true, true, R>
+                                  : k_trace_step<false, 64, T, M, false, true, R>);
   if (bps[k] < 0) {
     int b = 0;
     cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, kern, T, 0);

@@ -261,6 +261,51 @@ __device__ __forceinline__ uint32_t pop_wide(Trav& s, const uint2* stack) {
   return kSentinel;
 }
 
+// The 4-wide traversal stack in the thread's local memory.
+struct LocalStack {
+  uint2* a;
+  __device__ __forceinline__ void reset() {}
+  __device__ __forceinline__ void push(Trav& s, uint2 e) { a[s.sp++] = e; }
+  __device__ __forceinline__ uint32_t pop(Trav& s) { return pop_wide(s, a); }
+};
+
+// The same stack with its top K entries in a shared-memory ring (this
+// thread's slot j at ring[j * T], so that a warp's lanes hit consecutive
+// words) and older entries in local memory: pushes and pops, which sit on
+// the path from one node to the next, stay on chip.  The ring holds the
+// logical entries [lo, sp); a push into a full ring first moves entry lo out
+// to local memory, a pop below lo reads it back from there.
+template <int K, int T>
+struct RingStack {
+  static_assert((K & (K - 1)) == 0, "ring size must be a power of two");
+  uint2* ring;   // &shared[threadIdx.x]
+  uint2* spill;  // local array of the full stack capacity
+  int lo;
+  __device__ __forceinline__ void reset() { lo = 0; }
+  __device__ __forceinline__ void push(Trav& s, uint2 e) {
+    if (s.sp - lo == K) {
+      spill[lo] = ring[(lo & (K - 1)) * T];
+      ++lo;
+    }
+    ring[(s.sp & (K - 1)) * T] = e;
+    ++s.sp;
+  }
+  __device__ __forceinline__ uint32_t pop(Trav& s) {
+    while (s.sp > 0) {
+      --s.sp;
+      uint2 e;
+      if (s.sp >= lo) {
+        e = ring[(s.sp & (K - 1)) * T];
+      } else {
+        e = spill[s.sp];
+        lo = s.sp;
+      }
+      if (__uint_as_float(e.y) <= s.cull_hi) return e.x;
+    }
+    return kSentinel;
+  }
+};
+
 // Byte i of w as a float: the byte is placed under exponent 2^23 (0x4B000000)
 // and 2^23 subtracted, both exact.
 __device__ __forceinline__ float fmax3(float a, float b, float c) {
@@ -282,8 +327,8 @@ __device__ __forceinline__ float qbyte(uint32_t w) {
 // One 4-wide inner node: tests its children, pushes all hit children but the
 // nearest, and moves to the nearest (or pops).  Returns false on stack
 // overflow (s.sp = -1).
-template <int STACK>
-__device__ __forceinline__ bool visit_wide(const DeviceScene& S, Trav& s, uint2* stack) {
+template <int STACK, class Stk>
+__device__ __forceinline__ bool visit_wide_stk(const DeviceScene& S, Trav& s, Stk& stk) {
   s.nvis++;
   const float4 h = ldg4(S.inner, 4u * s.node + 0u);
   const float4 r = ldg4(S.inner, 4u * s.node + 1u);
@@ -326,18 +371,24 @@ __device__ __forceinline__ bool visit_wide(const DeviceScene& S, Trav& s, uint2*
   // t0 is the minimum; t2 (the other pair's minimum) is pushed last
   const int nh = (t0 < inf) + (t1 < inf) + (t2 < inf) + (t3 < inf);
   if (nh == 0) {
-    s.node = pop_wide(s, stack);
+    s.node = stk.pop(s);
   } else {
     if (s.sp + nh - 1 > STACK) {
       s.sp = -1;
       return false;
     }
-    if (t3 < inf) stack[s.sp++] = make_uint2(r3, __float_as_uint(t3));
-    if (t1 < inf) stack[s.sp++] = make_uint2(r1, __float_as_uint(t1));
-    if (t2 < inf) stack[s.sp++] = make_uint2(r2, __float_as_uint(t2));
+    if (t3 < inf) stk.push(s, make_uint2(r3, __float_as_uint(t3)));
+    if (t1 < inf) stk.push(s, make_uint2(r1, __float_as_uint(t1)));
+    if (t2 < inf) stk.push(s, make_uint2(r2, __float_as_uint(t2)));
     s.node = r0;
   }
   return true;
+}
+
+template <int STACK>
+__device__ __forceinline__ bool visit_wide(const DeviceScene& S, Trav& s, uint2* stack) {
+  LocalStack stk{stack};
+  return visit_wide_stk<STACK>(S, s, stk);
 }
 
 template <bool ANY, int STACK>

@@ -196,4 +196,5 @@ def test_pool_admission_without_a_gpu(rt):
         with pytest.raises(rt.RtError) as e:
             pool.trace([(0, None, None, 0)] * 9000)
         assert e.value.status == 1
-    assert rt.describe_pool_variant(0) == (128, 12)
+    assert rt.describe_pool_variant(0) == (128, 10, 16)
+    assert rt.describe_pool_variant(2) == (128, 12, 0)
