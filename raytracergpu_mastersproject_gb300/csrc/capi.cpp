@@ -246,8 +246,9 @@ rt_status rt_scene_create_ex(const RtSceneDesc* desc, rt_scene** out_scene) {
     build_bvh(wt.data(), nt, ws.data(), ns, desc->bvh_mode, sc->nodes40);
   }
   HostDeviceBVH hb;
-  uint32_t width = desc->node_width ? desc->node_width : kDefaultWidth;
-  if (width != 2 && width != 4) {
+  // 0 lets the conversion choose (4-wide unless the scene is too wide for it)
+  const uint32_t width = desc->node_width;
+  if (width != 0 && width != 2 && width != 4) {
     set_error("rt_scene_create_ex: node_width must be 0, 2 or 4");
     return RT_EINVAL;
   }

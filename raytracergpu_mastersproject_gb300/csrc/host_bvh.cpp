@@ -350,9 +350,22 @@ bool convert_bvh(const RtBVHNode40* nodes, uint32_t nn, const RtTriangle64* tris
                  const RtSphere32* sph, uint32_t ns, const RtMaterial32* mats, uint32_t nm,
                  uint32_t leaf_size, uint32_t width, HostDeviceBVH& out, std::string& msg) {
   out = HostDeviceBVH();
-  if (width == 0) width = kDefaultWidth;
+  // 4-wide nodes store per-axis steps 2^e with e <= kMaxWideExp (the kernels
+  // scale by 2^(e+15)); a root box wider than 255 * 2^kMaxWideExp (7.2e16)
+  // keeps the binary layout, or is rejected when 4-wide nodes were asked for.
+  bool too_wide = false;
+  if (nn > 0) {
+    const RtBVHNode40& r = nodes[0];
+    const double lim = 255.0 * std::ldexp(1.0, kMaxWideExp);
+    too_wide = (double)r.maxX - r.minX > lim || (double)r.maxY - r.minY > lim || (double)r.maxZ - r.minZ > lim;
+  }
+  if (width == 0) width = too_wide ? 2u : kDefaultWidth;
   if (width != 2 && width != 4) {
     msg = "node width must be 2 or 4";
+    return false;
+  }
+  if (width == 4 && too_wide) {
+    msg = "scene extent beyond 255 * 2^48 (7.2e16) needs node width 2";
     return false;
   }
   if (leaf_size == 0) leaf_size = kDefaultLeafSize;
@@ -585,7 +598,7 @@ bool convert_bvh(const RtBVHNode40* nodes, uint32_t nn, const RtTriangle64* tris
             while (255.0 * std::ldexp(1.0, e2) < ext) ++e2;
             while (e2 > -126 && 255.0 * std::ldexp(1.0, e2 - 1) >= ext) --e2;
           }
-          ex[a] = std::max(-126, std::min(127, e2));
+          ex[a] = std::max(-126, std::min(kMaxWideExp, e2));
         }
         uint32_t q[6] = {0, 0, 0, 0, 0, 0};  // qlo_x, qhi_x, qlo_y, qhi_y, qlo_z, qhi_z
         for (uint32_t j = w.count; j < 4; ++j)  // unused slot: qlo 255 > qhi 0, empty for any ray
@@ -605,7 +618,8 @@ bool convert_bvh(const RtBVHNode40* nodes, uint32_t nn, const RtTriangle64* tris
         }
         float* o = &out.inner[16 * i];
         o[0] = lo[0]; o[1] = lo[1]; o[2] = lo[2];
-        o[3] = bits_f((uint32_t)(ex[0] + 127) | ((uint32_t)(ex[1] + 127) << 8) | ((uint32_t)(ex[2] + 127) << 16) |
+        // exponent bytes hold e + 15 + 127: the kernels read 2^(e+15) directly
+        o[3] = bits_f((uint32_t)(ex[0] + 142) | ((uint32_t)(ex[1] + 142) << 8) | ((uint32_t)(ex[2] + 142) << 16) |
                       (w.count << 24));
         for (uint32_t j = 0; j < 4; ++j)
           o[4 + j] = bits_f(j < w.count ? ref_of(w.ch[j], dev) : (kLeafBit | kSphereBit | kSphereMask));

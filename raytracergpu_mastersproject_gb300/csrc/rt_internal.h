@@ -50,6 +50,9 @@ constexpr uint32_t kMaxTriangles = 1u << 27;
 constexpr uint32_t kSentinel = 0x7FFFFFFFu;  // stack bottom, never a node index
 constexpr uint32_t kDefaultLeafSize = 1;
 constexpr uint32_t kDefaultWidth = 4;
+// Largest quantisation step exponent of a 4-wide node: the kernels scale by
+// 2^(e+15) / d with |1/d| <= 2^64, which must stay below 2^128.
+constexpr int kMaxWideExp = 48;
 
 struct DeviceScene {
   const void* inner = nullptr;     // float4[4 * n_inner]

@@ -101,7 +101,10 @@ __device__ __forceinline__ void trav_set_close(Trav& s, float t) {
 __device__ __forceinline__ void trav_init_ray(Trav& s, const float4 o_tmin, const float4 d_tmax, uint32_t root) {
   s.ox = o_tmin.x; s.oy = o_tmin.y; s.oz = o_tmin.z; s.tmin = o_tmin.w;
   s.dx = d_tmax.x; s.dy = d_tmax.y; s.dz = d_tmax.z;
-  const float eps = 1e-30f;
+  // Zero (or smaller) direction components become +-2^-64, so 1/d stays
+  // within 2^64: with 4-wide steps up to 2^kMaxWideExp the node scale
+  // 2^(e+15)/d stays finite.
+  const float eps = 5.42101086242752217e-20f;  // 2^-64
   s.ix = 1.0f / (fabsf(s.dx) > eps ? s.dx : copysignf(eps, s.dx));
   s.iy = 1.0f / (fabsf(s.dy) > eps ? s.dy : copysignf(eps, s.dy));
   s.iz = 1.0f / (fabsf(s.dz) > eps ? s.dz : copysignf(eps, s.dz));
@@ -237,18 +240,21 @@ __device__ __forceinline__ bool trav_run(const DeviceScene& S, Trav& s, uint32_t
 
 // ------------------------------------------------------ 4-wide nodes ----
 // Node (64 B): float4 (p.xyz, meta), uint4 refs, uint4 (qlo_x, qhi_x, qlo_y,
-// qhi_y), uint4 (qlo_z, qhi_z, -, -); meta = exponent bytes ex|ey<<8|ez<<16
-// (biased by 127) | child count << 24.  Child i spans p + q*2^e per axis,
-// with q the i-th byte of the matching word.
+// qhi_y), uint4 (qlo_z, qhi_z, -, -); meta = exponent bytes (e + 15 + 127 per
+// axis) | child count << 24.  Child i spans p + q*2^e per axis, with q the
+// i-th byte of the matching word.
 //
-// A plane's parameter is fma(q, A, B) with A = 2^e/d (exact) and
-// B = (p - o)/d.  Against the exact value it is off by less than
-// 2 ulp of |t| plus 5 ulp of |B| (one rounding each for 1/d, p - o, the
-// product, B -/+ e and the fma).  Each axis therefore uses B - e for its near
-// plane and B + e for its far plane, e = |B| * 2^-21 (8 ulp), and the
-// resulting interval is widened by |t| * 2^-21.  The near plane of an axis is
-// the low bound when d >= 0 and the high bound otherwise, so no per-axis
-// min/max is needed.
+// A plane's parameter t = (p + q*2^e - o)/d is evaluated as one fma,
+// fma(Q, A, C) with Q = 1 + q*2^-15 (the byte placed in the mantissa under
+// 1.0f: one byte permute, exact), A = 2^(e+15)/d (exact scaling of 1/d) and
+// C = (p - o)/d - A per axis and node.  With B = (p - o)/d, the rounding of
+// 1/d, p - o, the product, B - A and the fma keep it within
+// 2^-24 (4|B| + 3|C| + 2.02|A|) of the exact value (|t| <= |C| + 1.008|A|).
+// Each axis therefore uses C - M for its near plane and C + M for its far
+// plane, with M = (|B| + |C| + |A|) * 2^-21 -- twice that bound and more, and
+// at most 1/64 of a quantisation step (|A| * 2^-21 = 2^e/|d| * 2^-6) beyond
+// the distance-relative terms.  The near plane of an axis is the low bound
+// when d >= 0 and the high bound otherwise, so no per-axis min/max is needed.
 constexpr float kWideWidenB = 4.76837158203125e-07f;  // 2^-21
 
 // Stack entries are (ref, t_near); an entry that starts beyond the closest
@@ -319,9 +325,11 @@ __device__ __forceinline__ float fmin3(float a, float b, float c) {
   return d;
 }
 
+// 1 + (byte I of w) * 2^-15: the byte becomes mantissa bits 8-15 under the
+// bits of 1.0f (0x3F800000), so the value is exact.
 template <int I>
 __device__ __forceinline__ float qbyte(uint32_t w) {
-  return __uint_as_float(__byte_perm(w, 0x4B000000u, (uint32_t)I | 0x7650u)) - 8388608.0f;
+  return __uint_as_float(__byte_perm(w, 0x3F800000u, 0x7604u | ((uint32_t)I << 4)));
 }
 
 // One 4-wide inner node: tests its children, pushes all hit children but the
@@ -339,9 +347,13 @@ __device__ __forceinline__ bool visit_wide_stk(const DeviceScene& S, Trav& s, St
   const float ay = __uint_as_float(((meta >> 8) & 0xFFu) << 23) * s.iy;
   const float az = __uint_as_float(((meta >> 16) & 0xFFu) << 23) * s.iz;
   const float bx = (h.x - s.ox) * s.ix, by = (h.y - s.oy) * s.iy, bz = (h.z - s.oz) * s.iz;
-  const float bxn = fmaf(-fabsf(bx), kWideWidenB, bx), bxf = fmaf(fabsf(bx), kWideWidenB, bx);
-  const float byn = fmaf(-fabsf(by), kWideWidenB, by), byf = fmaf(fabsf(by), kWideWidenB, by);
-  const float bzn = fmaf(-fabsf(bz), kWideWidenB, bz), bzf = fmaf(fabsf(bz), kWideWidenB, bz);
+  const float cx = bx - ax, cy = by - ay, cz = bz - az;
+  const float mx = (fabsf(bx) + fabsf(cx) + fabsf(ax)) * kWideWidenB;
+  const float my = (fabsf(by) + fabsf(cy) + fabsf(ay)) * kWideWidenB;
+  const float mz = (fabsf(bz) + fabsf(cz) + fabsf(az)) * kWideWidenB;
+  const float bxn = cx - mx, bxf = cx + mx;
+  const float byn = cy - my, byf = cy + my;
+  const float bzn = cz - mz, bzf = cz + mz;
   // near/far words per axis from the direction's sign; unused child slots
   // hold qlo = 255 > qhi = 0, an empty interval for either sign.
   const uint32_t nx = s.ix >= 0.0f ? fbits(qa.x) : fbits(qa.y), fx = s.ix >= 0.0f ? fbits(qa.y) : fbits(qa.x);
@@ -354,8 +366,8 @@ __device__ __forceinline__ bool visit_wide_stk(const DeviceScene& S, Trav& s, St
   {                                                                                               \
     float n = fmax3(fmaf(qbyte<I>(nx), ax, bxn), fmaf(qbyte<I>(ny), ay, byn), fmaf(qbyte<I>(nz), az, bzn)); \
     float f = fmin3(fmaf(qbyte<I>(fx), ax, bxf), fmaf(qbyte<I>(fy), ay, byf), fmaf(qbyte<I>(fz), az, bzf)); \
-    n = fmaxf(fmaf(-fabsf(n), kSlabWiden, n), s.cull_lo);                                         \
-    f = fminf(fmaf(fabsf(f), kSlabWiden, f), s.cull_hi);                                          \
+    n = fmaxf(n, s.cull_lo);                                                                      \
+    f = fminf(f, s.cull_hi);                                                                      \
     T = n <= f ? n : inf;                                                                         \
   }
   RT_CHILD(0, t0) RT_CHILD(1, t1) RT_CHILD(2, t2) RT_CHILD(3, t3)

@@ -287,3 +287,60 @@ def test_sorted_order_same_hits(rt, cuda, width):
         assert np.array_equal(a.view(np.uint64), b.view(np.uint64))
         c = sc.trace_host(rays[:300_000], sort=True)
         assert np.array_equal(c.view(np.uint64), dev_trace(rt, cuda, sc, rays[:300_000]).view(np.uint64))
+
+
+def _axis_rays(rt, n, scale, seed):
+    """Rays inside a cube of side `scale`, half of them along +-x/y/z exactly
+    (two zero direction components), the rest with one zero component."""
+    rng = np.random.default_rng(seed)
+    rays = np.zeros(n, rt.RAY_DTYPE)
+    o = rng.uniform(0.0, scale, (n, 3)).astype(np.float32)
+    d = rng.normal(size=(n, 3)).astype(np.float32)
+    axis = rng.integers(0, 3, n)
+    half = n // 2
+    d[:half] = 0.0
+    d[np.arange(half), axis[:half]] = rng.choice([-1.0, 1.0], half)
+    d[np.arange(half, n), axis[half:]] = 0.0
+    d /= np.sqrt((d.astype(np.float64) ** 2).sum(1, keepdims=True)).astype(np.float32)
+    rays["org"] = o
+    rays["tmin"] = 0.0
+    rays["dir"] = d
+    rays["tmax"] = np.float32(np.inf)
+    return rays
+
+
+@pytest.mark.parametrize("scale", [1.0, 1.0e7, 1.0e9])
+def test_axis_parallel_rays_at_large_scales(rt, orc, cuda, scale):
+    """Direction components of exactly 0 in scenes up to 1e9 wide (4-wide
+    steps up to 2^22; far beyond that the reference's own triangle test
+    overflows binary32): the node step's scale A = 2^(e+15)/d stays finite
+    and conservative, and both layouts match the oracle."""
+    tris = rt.gen_soup(31, 0, 30_000, 1.0, 0.01)
+    for k in ("v0", "v1", "v2"):
+        tris[k][:, :3] *= np.float32(scale)
+    rays = _axis_rays(rt, 40_000, scale, 5)
+    with rt.Scene(tris, node_width=4) as s4, rt.Scene(tris, node_width=2) as s2:
+        assert s4.info().node_width == 4
+        got4 = dev_trace(rt, cuda, s4, rays)
+        got2 = dev_trace(rt, cuda, s2, rays)
+        ref, _ = orc.trace(orc.Scene(tris, s4.nodes()), rays, canonical=True)
+    assert (ref["prim"] != orc.NO_HIT).sum() > 1000
+    assert_parity(orc, tris, rays, ref, got4)
+    assert_parity(orc, tris, rays, ref, got2)
+
+
+def test_extent_beyond_wide_range_uses_binary_nodes(rt, orc, cuda):
+    """Beyond 255 * 2^48 the 4-wide quantisation is not used: the default
+    layout falls back to binary nodes and an explicit width of 4 is refused."""
+    tris = rt.gen_soup(32, 0, 5_000, 1.0, 0.01)
+    for k in ("v0", "v1", "v2"):
+        tris[k][:, :3] *= np.float32(1.0e17)
+    rays = _axis_rays(rt, 10_000, 1.0e17, 6)
+    with rt.Scene(tris) as sc:
+        assert sc.info().node_width == 2
+        got = dev_trace(rt, cuda, sc, rays)
+        ref, _ = orc.trace(orc.Scene(tris, sc.nodes()), rays)
+    assert_parity(orc, tris, rays, ref, got)
+    with pytest.raises(rt.RtError) as e:
+        rt.Scene(tris, node_width=4)
+    assert e.value.status == 1
