@@ -256,3 +256,26 @@ np.save({repr(str(tmp_path / "b.npy"))}, acc.cpu().numpy())
     p = subprocess.run([sys.executable, "-c", code], env=env, capture_output=True, text=True, timeout=300)
     assert p.returncode == 0, p.stderr
     assert np.array_equal(np.load(tmp_path / "b.npy"), a)
+
+
+def test_deep_stack_render_matches_per_pixel(rt, cuda):
+    """A dense cluster of large triangles keeps traversal stacks far past the
+    shared-memory ring; the wavefront frame equals the binary per-pixel one."""
+    rng = np.random.default_rng(8)
+    n = 20_000
+    tris = np.zeros(n, rt.TRIANGLE_DTYPE)
+    c = rng.normal(0.0, 0.05, (n, 3)).astype(np.float32)
+    for k in ("v0", "v1", "v2"):
+        tris[k][:, :3] = c + rng.normal(0.0, 0.5, (n, 3)).astype(np.float32)
+    tris["materialIndex"] = rng.integers(0, 2, n)
+    mats = np.zeros(2, rt.MATERIAL_DTYPE)
+    mats[0]["albedo"][:3] = (0.6, 0.5, 0.4)
+    mats[0]["materialType"] = rt.MAT_DIFFUSE
+    mats[1]["albedo"][:3] = (2.0, 2.0, 2.0)
+    mats[1]["materialType"] = rt.MAT_LIGHT
+    ubo = rt.make_ubo((0.0, 0.0, 4.0), (0.0, 0.0, 0.0), fov=40.0, depth=4, random_state=9)
+    with rt.Scene(tris, materials=mats, node_width=2) as s2, rt.Scene(tris, materials=mats, node_width=4) as s4:
+        a = gpu_render(rt, cuda, s2, ubo, 64, 48, 3)
+        b = gpu_render(rt, cuda, s4, ubo, 64, 48, 3)
+    assert np.array_equal(a, b)
+    assert a[0::4].max() > 0.1

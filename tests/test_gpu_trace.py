@@ -344,3 +344,46 @@ def test_extent_beyond_wide_range_uses_binary_nodes(rt, orc, cuda):
     with pytest.raises(rt.RtError) as e:
         rt.Scene(tris, node_width=4)
     assert e.value.status == 1
+
+
+def _dense_cluster(rt, n, seed):
+    """n large triangles crossing one small region: rays through it test
+    thousands of boxes and keep deep traversal stacks."""
+    rng = np.random.default_rng(seed)
+    tris = np.zeros(n, rt.TRIANGLE_DTYPE)
+    c = rng.normal(0.0, 0.05, (n, 3)).astype(np.float32)
+    for k in ("v0", "v1", "v2"):
+        tris[k][:, :3] = c + rng.normal(0.0, 0.5, (n, 3)).astype(np.float32)
+    return tris
+
+
+def _rays_at_origin(rt, n, seed):
+    rng = np.random.default_rng(seed)
+    rays = np.zeros(n, rt.RAY_DTYPE)
+    o = rng.uniform(-3.0, 3.0, (n, 3)).astype(np.float32)
+    d = (-o + rng.normal(0.0, 0.1, (n, 3))).astype(np.float32)
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    rays["org"], rays["dir"], rays["tmin"], rays["tmax"] = o, d, 0.0, np.float32(np.inf)
+    return rays
+
+
+def test_deep_stacks_spill_the_shared_ring(rt, orc, cuda):
+    """About 5,500 box tests and 400 triangle tests per ray: traversal stacks
+    run far past the 16 entries each lane keeps in shared memory, so entries
+    move out to local memory and back.  Hits match the oracle for both ray
+    kinds, both node layouts and the sorted order."""
+    tris = _dense_cluster(rt, 20_000, 3)
+    rays = _rays_at_origin(rt, 20_000, 4)
+    with rt.Scene(tris, node_width=4) as s4, rt.Scene(tris, node_width=2) as s2:
+        assert s4.info().stack_need > 16
+        closest4 = dev_trace(rt, cuda, s4, rays)
+        sorted4 = dev_trace(rt, cuda, s4, rays, sort=True)
+        closest2 = dev_trace(rt, cuda, s2, rays)
+        any4 = dev_trace(rt, cuda, s4, rays, any_hit=True)
+        ref, st = orc.trace(orc.Scene(tris, s4.nodes()), rays, canonical=True)
+    assert st[0] / len(rays) > 1000  # boxes tested per ray
+    assert_parity(orc, tris, rays, ref, closest4)
+    assert_parity(orc, tris, rays, ref, closest2)
+    assert np.array_equal(closest4.view(np.uint64), sorted4.view(np.uint64))
+    hit = ref["prim"] != orc.NO_HIT
+    assert np.array_equal(any4["prim"] != orc.NO_HIT, hit)  # any-hit finds a hit exactly where one exists
