@@ -183,9 +183,11 @@ def workload(n_tris: int, n_rays: int):
     return tris, rays
 
 
-def cpu_leg(tris, nodes, rays, sample: int) -> tuple[dict, dict]:
-    """CPU baseline: the oracle's reference-order traversal on `sample` rays
-    with every host thread; plus canonical traversal counts (work per ray)."""
+def cpu_leg(tris, nodes, rays, sample: int, trav_nodes=None) -> tuple[dict, dict]:
+    """CPU baseline: the oracle's reference-order traversal of the S1 tree
+    (`nodes`, the reference's own) on `sample` rays with every host thread;
+    plus canonical traversal counts (work per ray) on the tree the kernel
+    traverses (`trav_nodes`, default the S1 tree)."""
     from oracle import oracle as orc
 
     orc.build()
@@ -196,8 +198,9 @@ def cpu_leg(tris, nodes, rays, sample: int) -> tuple[dict, dict]:
     ref_hits, st = orc.trace(S, sub, canonical=False, nthreads=cores)
     dt = time.perf_counter() - t0
     cnt = sub
+    St = S if trav_nodes is None else orc.Scene(tris, trav_nodes)
     t1 = time.perf_counter()
-    can_hits, cst = orc.trace(S, cnt, canonical=True, nthreads=cores)
+    can_hits, cst = orc.trace(St, cnt, canonical=True, nthreads=cores)
     dt_can = time.perf_counter() - t1
     counts = {"node_boxes_per_ray": float(cst[0]) / len(cnt), "tri_tests_per_ray": float(cst[1]) / len(cnt),
               "sample": len(cnt)}
@@ -206,8 +209,9 @@ def cpu_leg(tris, nodes, rays, sample: int) -> tuple[dict, dict]:
                       f"(reference order, no culling, sorted-leaf BVH), {cores} threads, {dt:.2f} s",
             "canonical": {"value": len(cnt) / dt_can / 1e9, "unit": UNIT, "cores": cores,
                           "sample": f"first {len(cnt)} rays, the same restatement with near-child-first "
-                                    f"order and interval culling (the kernels' order; same hits), "
-                                    f"{dt_can:.2f} s"}}
+                                    f"order and interval culling (the kernels' order; same hits) over "
+                                    f"{'the binned-SAH tree the kernel traverses' if trav_nodes is not None else 'the S1 tree'}"
+                                    f", {dt_can:.2f} s"}}
     return base, {"counts": counts, "ref_hits": ref_hits, "can_hits": can_hits}
 
 
@@ -532,7 +536,8 @@ def run_ours(args):
     cpu_base, counts, parity = None, None, None
     if not args.no_cpu:
         nodes = scene.nodes()
-        cpu_base, extra = cpu_leg(tris, nodes, rays, min(args.cpu_sample, n))
+        trav = rt.build_bvh_sah(tris) if info.traversal_sah else None
+        cpu_base, extra = cpu_leg(tris, nodes, rays, min(args.cpu_sample, n), trav)
         counts = extra["counts"]
         got = d_hits.cpu().numpy().view(rt.HIT_DTYPE)
         k = len(extra["ref_hits"])
@@ -561,7 +566,8 @@ def run_ours(args):
             "config": {"workload": "config 3: 4,194,304-triangle soup, 16,777,216 incoherent rays, closest-hit"
                        if (args.tris, args.rays) == (N_TRIS, N_RAYS) else
                        f"config-3 shape: {args.tris} triangles, {args.rays} rays, closest-hit",
-                       "triangles": args.tris, "rays": n, "bvh": "host LBVH, sorted leaves",
+                       "triangles": args.tris, "rays": n, "bvh": ("S1 nodes: host LBVH, sorted leaves; traversed: binned-SAH tree over the same triangles"
+                               if info.traversal_sah else "host LBVH, sorted leaves (traversed as built)"),
                        "leaf_size": info.leaf_size, "node_width": info.node_width,
                        "device_nodes": info.device_nodes, "bvh_depth": info.depth, "stack_need": info.stack_need,
                        "l2": l2_note(n, info),

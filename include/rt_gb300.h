@@ -166,10 +166,19 @@ typedef struct RtSceneDesc {
   uint32_t bvh_mode;              /* RT_BVH_SORTED | RT_BVH_REFERENCE */
   uint32_t leaf_size;             /* max triangles per device leaf after collapsing; 0 = default (1) */
   uint32_t node_width;            /* device BVH width: 2 (binary) or 4 (quantised); 0 = default (4) */
-  uint32_t build_flags;           /* RT_BUILD_ON_DEVICE: build the node array with rt_build_bvh_device */
+  uint32_t build_flags;           /* RT_BUILD_ON_DEVICE | RT_BUILD_TRAVERSE_S1 */
 } RtSceneDesc;
 
+/* Build the node array with rt_build_bvh_device (the S1 passes on the GPU). */
 #define RT_BUILD_ON_DEVICE 1u
+/* Which tree the device traverses.  The scene always keeps the S1 node array
+ * (rt_scene_get_nodes).  When the library builds that array on the host in
+ * RT_BVH_SORTED mode, the device by default traverses a binned-SAH tree over
+ * the same primitives instead, built on the host: about 10% fewer box tests
+ * per ray, and the same hits (closest hits do not depend on the tree).  With
+ * this flag, and always for caller-supplied nodes, RT_BVH_REFERENCE or
+ * RT_BUILD_ON_DEVICE, it traverses the S1 array itself. */
+#define RT_BUILD_TRAVERSE_S1 2u
 
 typedef struct RtSceneInfo {
   uint32_t num_triangles;
@@ -184,6 +193,8 @@ typedef struct RtSceneInfo {
   double build_seconds;        /* host BVH build + conversion time */
   uint32_t node_width;         /* 2 or 4 */
   uint32_t stack_need;         /* worst-case traversal stack entries */
+  uint32_t traversal_sah;      /* 1: the device traverses the SAH tree; 0: the S1 array */
+  uint32_t _reserved;
 } RtSceneInfo;
 
 /* Replaces the scene upload + S1 BVH build of the reference
@@ -208,6 +219,15 @@ rt_status rt_build_bvh(const RtTriangle64* triangles, uint32_t num_triangles,
                        const RtSphere32* spheres, uint32_t num_spheres,
                        const RtModel64* models, uint32_t num_models,
                        uint32_t bvh_mode, RtBVHNode40* out_nodes);
+/* A binned surface-area-heuristic tree over the same primitives (triangles,
+ * then spheres; world space when models are given), 2N-1 nodes in the
+ * RtBVHNode40 form: root 0, leaves with left == right == 0 holding one
+ * primitive each.  Not the reference's leaf layout -- it is the tree the
+ * device traverses by default; passing it as RtSceneDesc.nodes traverses it
+ * too.  No counterpart in the reference. */
+rt_status rt_build_bvh_sah(const RtTriangle64* triangles, uint32_t num_triangles, const RtSphere32* spheres,
+                           uint32_t num_spheres, const RtModel64* models, uint32_t num_models,
+                           RtBVHNode40* out_nodes);
 
 /* The same six S1 passes on the GPU (device in, device out), bit-identical to
  * rt_build_bvh: centroid box, 30-bit Morton codes, stable radix sort of
@@ -456,6 +476,12 @@ const char* rt_last_error_string(void);
 uint32_t rt_abi_version(void);
 /* Waits for the stream with a deadline; RT_ETIMEOUT when it runs out. */
 rt_status rt_stream_wait(void* stream, double timeout_seconds);
+/* Frees the device workspace the library keeps for this stream on the current
+ * device (work counters, ray staging, reorder and path-tracing scratch), after
+ * the stream's work has finished.  No call on the stream may run concurrently;
+ * a later call on it allocates a new workspace.  No counterpart in the
+ * reference. */
+rt_status rt_stream_release(void* stream);
 
 #ifdef __cplusplus
 }

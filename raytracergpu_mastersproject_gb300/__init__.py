@@ -75,13 +75,15 @@ class _SceneDesc(C.Structure):
                 ("node_width", C.c_uint32), ("build_flags", C.c_uint32)]
 
 BUILD_ON_DEVICE = 1
+BUILD_TRAVERSE_S1 = 2
 
 
 class SceneInfo(C.Structure):
     _fields_ = [("num_triangles", C.c_uint32), ("num_spheres", C.c_uint32), ("num_materials", C.c_uint32),
                 ("num_nodes", C.c_uint32), ("device_nodes", C.c_uint32), ("depth", C.c_uint32),
                 ("leaf_size", C.c_uint32), ("bvh_mode", C.c_uint32), ("device_bytes", C.c_uint64),
-                ("build_seconds", C.c_double), ("node_width", C.c_uint32), ("stack_need", C.c_uint32)]
+                ("build_seconds", C.c_double), ("node_width", C.c_uint32), ("stack_need", C.c_uint32),
+                ("traversal_sah", C.c_uint32), ("_reserved", C.c_uint32)]
 
 
 class PoolOptions(C.Structure):
@@ -138,6 +140,7 @@ SIGNATURES = {
     "rt_scene_get_info": (_I, [_P, C.POINTER(SceneInfo)]),
     "rt_scene_get_nodes": (_I, [_P, _P, _U32]),
     "rt_build_bvh": (_I, [_P, _U32, _P, _U32, _P, _U32, _U32, _P]),
+    "rt_build_bvh_sah": (_I, [_P, _U32, _P, _U32, _P, _U32, _P]),
     "rt_build_bvh_device": (_I, [_P, _U32, _P, _U32, _U32, _P, _P]),
     "rt_trace": (_I, [_P, _P, _U32, _P, _U32, _P]),
     "rt_trace_host": (_I, [_P, _P, _U32, _P, _U32, _P]),
@@ -150,6 +153,7 @@ SIGNATURES = {
     "rt_last_error_string": (C.c_char_p, []),
     "rt_abi_version": (_U32, []),
     "rt_stream_wait": (_I, [_P, _D]),
+    "rt_stream_release": (_I, [_P]),
     "rt_pool_create": (_I, [C.POINTER(PoolOptions), C.POINTER(C.c_void_p)]),
     "rt_pool_destroy": (_I, [_P]),
     "rt_pool_add_scene": (_I, [_P, C.POINTER(_SceneDesc), C.POINTER(_U32)]),
@@ -241,10 +245,14 @@ class Scene:
     bvh_mode: BVH_SORTED (default) or BVH_REFERENCE (the reference's leaf order)
     leaf_size: max triangles per device leaf (1..8); 0 = library default
     node_width: device BVH width, 2 (binary) or 4 (quantised 4-wide); 0 = library default
+    build_on_device: build the S1 node array on the GPU (rt_build_bvh_device)
+    traverse_s1: traverse the S1 node array instead of the binned-SAH tree the
+        library otherwise builds for sorted-mode scenes (same hits)
     """
 
     def __init__(self, triangles, spheres=None, materials=None, models=None, nodes=None,
-                 bvh_mode: int = BVH_SORTED, leaf_size: int = 0, node_width: int = 0, build_on_device: bool = False):
+                 bvh_mode: int = BVH_SORTED, leaf_size: int = 0, node_width: int = 0, build_on_device: bool = False,
+                 traverse_s1: bool = False):
         L = lib()
         tri = np.ascontiguousarray(triangles, dtype=TRIANGLE_DTYPE) if triangles is not None else np.zeros(0, TRIANGLE_DTYPE)
         sph = np.ascontiguousarray(spheres, dtype=SPHERE_DTYPE) if spheres is not None else np.zeros(0, SPHERE_DTYPE)
@@ -253,7 +261,8 @@ class Scene:
         nod = np.ascontiguousarray(nodes, dtype=NODE_DTYPE) if nodes is not None else None
         d = _SceneDesc(_ptr(tri), len(tri), _ptr(sph), len(sph), _ptr(mat), len(mat),
                        _ptr(mod), 0 if mod is None else len(mod), _ptr(nod), 0 if nod is None else len(nod),
-                       bvh_mode, leaf_size, node_width, BUILD_ON_DEVICE if build_on_device else 0)
+                       bvh_mode, leaf_size, node_width,
+                       (BUILD_ON_DEVICE if build_on_device else 0) | (BUILD_TRAVERSE_S1 if traverse_s1 else 0))
         h = C.c_void_p()
         _check(L.rt_scene_create_ex(C.byref(d), C.byref(h)), "rt_scene_create_ex")
         self._h = h
@@ -539,6 +548,11 @@ class Server:
         self.close()
 
 
+def release_stream(stream=None) -> None:
+    """Frees the library's device workspace for `stream` (after its work ends)."""
+    _check(lib().rt_stream_release(_stream_handle(stream)), "rt_stream_release")
+
+
 def describe_pool_variant(v: int) -> tuple[int, int, int]:
     """-> (threads per block, minimum blocks per SM, stack entries per lane in shared memory)."""
     t, m, r = C.c_uint32(), C.c_uint32(), C.c_uint32()
@@ -555,6 +569,19 @@ def build_bvh(triangles, spheres=None, models=None, bvh_mode: int = BVH_SORTED) 
     out = np.zeros(max(2 * n - 1, 0), NODE_DTYPE)
     _check(lib().rt_build_bvh(_ptr(tri), len(tri), _ptr(sph), len(sph), _ptr(mod), 0 if mod is None else len(mod),
                               bvh_mode, _ptr(out)), "rt_build_bvh")
+    return out
+
+
+def build_bvh_sah(triangles, spheres=None, models=None) -> np.ndarray:
+    """The binned-SAH traversal tree -> NODE_DTYPE array of 2N-1 nodes (root 0;
+    not the reference's leaf layout)."""
+    tri = np.ascontiguousarray(triangles, dtype=TRIANGLE_DTYPE)
+    sph = np.ascontiguousarray(spheres, dtype=SPHERE_DTYPE) if spheres is not None else np.zeros(0, SPHERE_DTYPE)
+    mod = np.ascontiguousarray(models, dtype=MODEL_DTYPE) if models is not None else None
+    n = len(tri) + len(sph)
+    out = np.zeros(max(2 * n - 1, 0), NODE_DTYPE)
+    _check(lib().rt_build_bvh_sah(_ptr(tri), len(tri), _ptr(sph), len(sph), _ptr(mod),
+                                  0 if mod is None else len(mod), _ptr(out)), "rt_build_bvh_sah")
     return out
 
 

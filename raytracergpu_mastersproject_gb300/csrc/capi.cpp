@@ -181,6 +181,35 @@ rt_status rt_stream_wait(void* stream, double timeout_seconds) {
   }
 }
 
+rt_status rt_stream_release(void* stream) {
+  cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return cuda_fail(e, "rt_stream_release: cudaGetDevice");
+  Workspace* w = nullptr;
+  {
+    std::lock_guard<std::mutex> lk(g_ws_mu);
+    auto it = g_ws.find(std::make_pair(dev, st));
+    if (it == g_ws.end()) return RT_OK;
+    w = it->second;
+    g_ws.erase(it);
+  }
+  // the library's work on the stream (and on its helper streams) ends first
+  e = cudaStreamSynchronize(st);
+  for (cudaStream_t h : {w->copy_in, w->copy_out, w->trace2})
+    if (h) {
+      const cudaError_t e2 = cudaStreamSynchronize(h);
+      if (e == cudaSuccess) e = e2;
+      cudaStreamDestroy(h);
+    }
+  for (cudaEvent_t ev : w->ev)
+    if (ev) cudaEventDestroy(ev);
+  for (void* p : {static_cast<void*>(w->counters), w->stage, w->sort, w->wave})
+    if (p) cudaFree(p);
+  delete w;
+  return e == cudaSuccess ? RT_OK : cuda_fail(e, "rt_stream_release");
+}
+
 rt_status rt_build_bvh(const RtTriangle64* triangles, uint32_t num_triangles, const RtSphere32* spheres,
                        uint32_t num_spheres, const RtModel64* models, uint32_t num_models, uint32_t bvh_mode,
                        RtBVHNode40* out_nodes) {
@@ -199,6 +228,27 @@ rt_status rt_build_bvh(const RtTriangle64* triangles, uint32_t num_triangles, co
   }
   std::vector<RtBVHNode40> nodes;
   build_bvh(wt.data(), num_triangles, ws.data(), num_spheres, bvh_mode, nodes);
+  if (!nodes.empty()) std::memcpy(out_nodes, nodes.data(), nodes.size() * sizeof(RtBVHNode40));
+  return RT_OK;
+}
+
+rt_status rt_build_bvh_sah(const RtTriangle64* triangles, uint32_t num_triangles, const RtSphere32* spheres,
+                           uint32_t num_spheres, const RtModel64* models, uint32_t num_models,
+                           RtBVHNode40* out_nodes) {
+  const uint64_t N = (uint64_t)num_triangles + num_spheres;
+  if ((num_triangles && !triangles) || (num_spheres && !spheres) || (N && !out_nodes) || N > kMaxTriangles) {
+    set_error("rt_build_bvh_sah: bad argument");
+    return RT_EINVAL;
+  }
+  std::vector<RtTriangle64> wt;
+  std::vector<RtSphere32> ws;
+  std::string msg;
+  if (!world_space(triangles, num_triangles, spheres, num_spheres, models, num_models, wt, ws, msg)) {
+    set_error("rt_build_bvh_sah: " + msg);
+    return RT_EINVAL;
+  }
+  std::vector<RtBVHNode40> nodes;
+  build_sah(wt.data(), num_triangles, ws.data(), num_spheres, nodes);
   if (!nodes.empty()) std::memcpy(out_nodes, nodes.data(), nodes.size() * sizeof(RtBVHNode40));
   return RT_OK;
 }
@@ -227,6 +277,10 @@ rt_status rt_scene_create_ex(const RtSceneDesc* desc, rt_scene** out_scene) {
     set_error("rt_scene_create_ex: num_nodes must be 2*(triangles+spheres)-1");
     return RT_EINVAL;
   }
+  if (desc->build_flags & ~(RT_BUILD_ON_DEVICE | RT_BUILD_TRAVERSE_S1)) {
+    set_error("rt_scene_create_ex: unknown build_flags");
+    return RT_EINVAL;
+  }
   const auto t0 = std::chrono::steady_clock::now();
   std::unique_ptr<rt_scene> sc(new rt_scene());
   cudaGetDevice(&sc->device);
@@ -252,13 +306,19 @@ rt_status rt_scene_create_ex(const RtSceneDesc* desc, rt_scene** out_scene) {
     set_error("rt_scene_create_ex: node_width must be 0, 2 or 4");
     return RT_EINVAL;
   }
-  if (!convert_bvh(sc->nodes40.data(), (uint32_t)sc->nodes40.size(), wt.data(), nt, ws.data(), ns, desc->materials, nm,
+  // the traversal tree: SAH for library-built sorted-mode scenes, else S1
+  std::vector<RtBVHNode40> sah;
+  const bool use_sah = !desc->nodes && !(desc->build_flags & (RT_BUILD_ON_DEVICE | RT_BUILD_TRAVERSE_S1)) &&
+                       desc->bvh_mode == RT_BVH_SORTED && N > 1;
+  if (use_sah) build_sah(wt.data(), nt, ws.data(), ns, sah);
+  const std::vector<RtBVHNode40>& trav = use_sah ? sah : sc->nodes40;
+  if (!convert_bvh(trav.data(), (uint32_t)trav.size(), wt.data(), nt, ws.data(), ns, desc->materials, nm,
                    desc->leaf_size, width, hb, msg)) {
     set_error("rt_scene_create_ex: " + msg);
     return RT_EINVAL;
   }
   if (hb.width == 4 && hb.stack_need > 192u) {  // too deep for the wide stack: binary form
-    if (!convert_bvh(sc->nodes40.data(), (uint32_t)sc->nodes40.size(), wt.data(), nt, ws.data(), ns, desc->materials,
+    if (!convert_bvh(trav.data(), (uint32_t)trav.size(), wt.data(), nt, ws.data(), ns, desc->materials,
                      nm, desc->leaf_size, 2, hb, msg)) {
       set_error("rt_scene_create_ex: " + msg);
       return RT_EINVAL;
@@ -331,6 +391,7 @@ rt_status rt_scene_create_ex(const RtSceneDesc* desc, rt_scene** out_scene) {
   inf.build_seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
   inf.node_width = hb.width;
   inf.stack_need = hb.stack_need;
+  inf.traversal_sah = use_sah ? 1u : 0u;
   *out_scene = sc.release();
   return RT_OK;
 }

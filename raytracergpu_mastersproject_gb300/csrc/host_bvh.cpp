@@ -326,6 +326,333 @@ void build_bvh(const RtTriangle64* tris, uint32_t nt, const RtSphere32* sph, uin
 }
 
 // triangleHit's vertex-only values (raytraceBVH.comp:119-125), binary32.
+// ------------------------------------------------ SAH traversal tree ----
+// A binned surface-area-heuristic tree over the same primitives, in the node
+// form convert_bvh reads (root 0, leaves with left == right == 0, one
+// primitive per leaf).  Used for traversal only: closest hits do not depend
+// on the tree, and the scene keeps the reference-layout nodes for export.
+//
+// Primitive records (bounds, centroid, id) are kept in tree order and
+// partitioned in place, so every pass streams through memory.  A split bins
+// the range's centroids into kSahBins bins on all three axes and takes the
+// bin boundary of least  area(L) * |L| + area(R) * |R|; ranges of at most
+// kSahSweep primitives are sorted along their widest centroid axis and take
+// the exact split of that axis; a range whose centroids coincide is split in
+// the middle, and past kSahDepth levels every split is at the centroid
+// median, which bounds the depth.  The top of the tree is built with binning
+// and partitioning spread over the host threads, subtrees below kSahTask
+// primitives as parallel tasks.
+namespace {
+
+constexpr int kSahBins = 32;
+constexpr size_t kSahTask = 1u << 15;
+constexpr int kSahDepth = 48;
+constexpr size_t kSahSweep = 16;
+
+struct SahRec {
+  float lo[3], hi[3], c[3];
+  uint32_t id;
+};
+
+struct SahBox {
+  float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+  void grow(const float* l, const float* h) {
+    for (int a = 0; a < 3; ++a) {
+      lo[a] = l[a] < lo[a] ? l[a] : lo[a];
+      hi[a] = h[a] > hi[a] ? h[a] : hi[a];
+    }
+  }
+  void grow(const SahBox& b) { grow(b.lo, b.hi); }
+  double area() const {
+    const double dx = std::fmax(0.0, (double)hi[0] - lo[0]), dy = std::fmax(0.0, (double)hi[1] - lo[1]),
+                 dz = std::fmax(0.0, (double)hi[2] - lo[2]);
+    return dx * dy + dy * dz + dz * dx;
+  }
+};
+
+struct SahBin {
+  SahBox box;
+  uint32_t count = 0;
+};
+
+struct SahBuild {
+  uint32_t nt = 0;
+  std::vector<SahRec> rec, tmp;
+  std::vector<RtBVHNode40>* out = nullptr;
+  std::atomic<uint32_t> next{1};
+
+  static void set_box(RtBVHNode40& nd, const SahBox& b) {
+    nd.minX = b.lo[0]; nd.maxX = b.hi[0];
+    nd.minY = b.lo[1]; nd.maxY = b.hi[1];
+    nd.minZ = b.lo[2]; nd.maxZ = b.hi[2];
+  }
+  void leaf(uint32_t node, const SahRec& r) {
+    RtBVHNode40& nd = (*out)[node];
+    SahBox b;
+    b.grow(r.lo, r.hi);
+    set_box(nd, b);
+    nd.left = nd.right = 0;
+    if (r.id < nt) {
+      nd.primitiveIndex = r.id;
+      nd.primitiveType = RT_PRIM_TRIANGLE;
+    } else {
+      nd.primitiveIndex = r.id - nt;
+      nd.primitiveType = RT_PRIM_SPHERE;
+    }
+  }
+  void bounds(size_t b, size_t e, bool par, SahBox& box, SahBox& cb) const {
+    auto part = [&](size_t i0, size_t i1, SahBox& bx, SahBox& cx) {
+      for (size_t i = i0; i < i1; ++i) {
+        bx.grow(rec[i].lo, rec[i].hi);
+        cx.grow(rec[i].c, rec[i].c);
+      }
+    };
+    if (!par) {
+      part(b, e, box, cb);
+      return;
+    }
+    std::vector<SahBox> bx(host_threads()), cx(host_threads());
+    parallel_for(e - b, [&](size_t i0, size_t i1, unsigned t) { part(b + i0, b + i1, bx[t], cx[t]); });
+    for (size_t t = 0; t < bx.size(); ++t) {
+      box.grow(bx[t]);
+      cb.grow(cx[t]);
+    }
+  }
+  // Moves the records of [b, e) for which `left` holds to the front, in
+  // parallel through the scratch array when `par`; returns the split point.
+  template <class P>
+  size_t partition(size_t b, size_t e, bool par, P left) {
+    if (!par) {
+      SahRec* m = std::partition(rec.data() + b, rec.data() + e, left);
+      return (size_t)(m - rec.data());
+    }
+    const unsigned T = host_threads();
+    const size_t n = e - b, per = (n + T - 1) / T;
+    std::vector<size_t> nl(T, 0), nr(T, 0);
+    std::vector<std::thread> th;
+    for (unsigned t = 0; t < T; ++t)
+      th.emplace_back([&, t] {
+        const size_t i0 = b + std::min(n, t * per), i1 = b + std::min(n, (t + 1) * per);
+        for (size_t i = i0; i < i1; ++i) (left(rec[i]) ? nl[t] : nr[t])++;
+      });
+    for (auto& x : th) x.join();
+    th.clear();
+    size_t total_l = 0;
+    for (unsigned t = 0; t < T; ++t) total_l += nl[t];
+    std::vector<size_t> ol(T), orr(T);
+    size_t accl = b, accr = b + total_l;
+    for (unsigned t = 0; t < T; ++t) {
+      ol[t] = accl;
+      orr[t] = accr;
+      accl += nl[t];
+      accr += nr[t];
+    }
+    for (unsigned t = 0; t < T; ++t)
+      th.emplace_back([&, t] {
+        const size_t i0 = b + std::min(n, t * per), i1 = b + std::min(n, (t + 1) * per);
+        size_t l = ol[t], r = orr[t];
+        for (size_t i = i0; i < i1; ++i) tmp[left(rec[i]) ? l++ : r++] = rec[i];
+      });
+    for (auto& x : th) x.join();
+    parallel_for(n, [&](size_t i0, size_t i1, unsigned) {
+      std::memcpy(&rec[b + i0], &tmp[b + i0], (i1 - i0) * sizeof(SahRec));
+    });
+    return b + total_l;
+  }
+  // Splits [b, e), fills the node's box and returns the split point.
+  size_t split(uint32_t node, size_t b, size_t e, bool par, int depth) {
+    SahBox box, cb;
+    bounds(b, e, par, box, cb);
+    set_box((*out)[node], box);
+    const size_t n = e - b;
+    int wide = 0;
+    for (int k = 1; k < 3; ++k)
+      if (cb.hi[k] - cb.lo[k] > cb.hi[wide] - cb.lo[wide]) wide = k;
+    auto by_axis = [wide](const SahRec& p, const SahRec& q) { return p.c[wide] < q.c[wide]; };
+    if (depth >= kSahDepth) {
+      const size_t mid = b + n / 2;
+      std::nth_element(rec.begin() + (ptrdiff_t)b, rec.begin() + (ptrdiff_t)mid, rec.begin() + (ptrdiff_t)e, by_axis);
+      return mid;
+    }
+    if (n <= kSahSweep) {
+      std::sort(rec.begin() + (ptrdiff_t)b, rec.begin() + (ptrdiff_t)e, by_axis);
+      double right[kSahSweep];
+      SahBox acc;
+      for (size_t i = n - 1; i > 0; --i) {
+        acc.grow(rec[b + i].lo, rec[b + i].hi);
+        right[i] = acc.area() * (double)(n - i);
+      }
+      acc = SahBox();
+      double best = INFINITY;
+      size_t at = n / 2;
+      for (size_t i = 1; i < n; ++i) {
+        acc.grow(rec[b + i - 1].lo, rec[b + i - 1].hi);
+        const double c = acc.area() * (double)i + right[i];
+        if (c < best) {
+          best = c;
+          at = i;
+        }
+      }
+      return b + at;
+    }
+    float scale[3];
+    for (int a = 0; a < 3; ++a) {
+      const float ext = cb.hi[a] - cb.lo[a];
+      scale[a] = ext > 0.0f ? (float)kSahBins / ext : 0.0f;
+    }
+    auto bin_of = [&](const SahRec& p, int a) {
+      const int k = (int)((p.c[a] - cb.lo[a]) * scale[a]);
+      return k < 0 ? 0 : (k >= kSahBins ? kSahBins - 1 : k);
+    };
+    auto fill = [&](size_t i0, size_t i1, SahBin (*bins)[kSahBins]) {
+      for (size_t i = i0; i < i1; ++i)
+        for (int a = 0; a < 3; ++a)
+          if (scale[a] > 0.0f) {
+            SahBin& bn = bins[a][bin_of(rec[i], a)];
+            bn.box.grow(rec[i].lo, rec[i].hi);
+            bn.count++;
+          }
+    };
+    SahBin bins[3][kSahBins];
+    if (!par) {
+      fill(b, e, bins);
+    } else {
+      std::vector<SahBin> tb((size_t)host_threads() * 3 * kSahBins);
+      parallel_for(n, [&](size_t i0, size_t i1, unsigned t) {
+        fill(b + i0, b + i1, reinterpret_cast<SahBin(*)[kSahBins]>(&tb[(size_t)t * 3 * kSahBins]));
+      });
+      for (unsigned t = 0; t < host_threads(); ++t)
+        for (int a = 0; a < 3; ++a)
+          for (int k = 0; k < kSahBins; ++k) {
+            const SahBin& x = tb[((size_t)t * 3 + a) * kSahBins + k];
+            if (x.count) {
+              bins[a][k].box.grow(x.box);
+              bins[a][k].count += x.count;
+            }
+          }
+    }
+    double best = INFINITY;
+    int best_axis = -1, best_k = 0;
+    for (int a = 0; a < 3; ++a) {
+      if (scale[a] <= 0.0f) continue;
+      double right_area[kSahBins];
+      uint32_t right_count[kSahBins];
+      SahBox acc;
+      uint32_t cnt = 0;
+      for (int k = kSahBins - 1; k > 0; --k) {
+        if (bins[a][k].count) acc.grow(bins[a][k].box);
+        cnt += bins[a][k].count;
+        right_area[k] = acc.area();
+        right_count[k] = cnt;
+      }
+      acc = SahBox();
+      cnt = 0;
+      for (int k = 0; k < kSahBins - 1; ++k) {
+        if (bins[a][k].count) acc.grow(bins[a][k].box);
+        cnt += bins[a][k].count;
+        if (cnt == 0 || right_count[k + 1] == 0) continue;
+        const double c = acc.area() * cnt + right_area[k + 1] * right_count[k + 1];
+        if (c < best) {
+          best = c;
+          best_axis = a;
+          best_k = k;
+        }
+      }
+    }
+    if (best_axis < 0) return b + n / 2;  // coincident centroids
+    const int a = best_axis, k = best_k;
+    const size_t mid = partition(b, e, par, [&](const SahRec& p) { return bin_of(p, a) <= k; });
+    return mid == b || mid == e ? b + n / 2 : mid;
+  }
+  void children(uint32_t node, uint32_t& l, uint32_t& r) {
+    const uint32_t c = next.fetch_add(2);
+    l = c;
+    r = c + 1;
+    (*out)[node].left = l;
+    (*out)[node].right = r;
+    (*out)[node].primitiveIndex = 0;
+    (*out)[node].primitiveType = 0;
+  }
+  void build_serial(uint32_t node, size_t b, size_t e, int depth) {
+    if (e - b == 1) {
+      leaf(node, rec[b]);
+      return;
+    }
+    const size_t mid = split(node, b, e, false, depth);
+    uint32_t l, r;
+    children(node, l, r);
+    build_serial(l, b, mid, depth + 1);
+    build_serial(r, mid, e, depth + 1);
+  }
+};
+
+}  // namespace
+
+void build_sah(const RtTriangle64* tris, uint32_t nt, const RtSphere32* sph, uint32_t ns,
+               std::vector<RtBVHNode40>& out) {
+  const size_t N = (size_t)nt + ns;
+  out.assign(N ? 2 * N - 1 : 0, RtBVHNode40{});
+  if (N == 0) return;
+  SahBuild B;
+  B.nt = nt;
+  B.out = &out;
+  B.rec.resize(N);
+  if (N > kSahTask) B.tmp.resize(N);
+  parallel_for(N, [&](size_t b, size_t e, unsigned) {
+    for (size_t i = b; i < e; ++i) {
+      SahRec& r = B.rec[i];
+      if (i < nt) {
+        const RtTriangle64& T = tris[i];
+        for (int a = 0; a < 3; ++a) {
+          r.lo[a] = std::fmin(std::fmin(T.v0[a], T.v1[a]), T.v2[a]);
+          r.hi[a] = std::fmax(std::fmax(T.v0[a], T.v1[a]), T.v2[a]);
+        }
+      } else {
+        const RtSphere32& S = sph[i - nt];
+        for (int a = 0; a < 3; ++a) {
+          r.lo[a] = S.center[a] - S.radius;
+          r.hi[a] = S.center[a] + S.radius;
+        }
+      }
+      for (int a = 0; a < 3; ++a) r.c[a] = 0.5f * r.lo[a] + 0.5f * r.hi[a];
+      r.id = (uint32_t)i;
+    }
+  });
+  // Top of the tree: breadth-first with the passes spread over the threads,
+  // until every open range is small enough to be a task of its own.
+  struct Range {
+    uint32_t node;
+    size_t b, e;
+    int depth;
+  };
+  std::vector<Range> open{{0u, 0, N, 0}}, tasks;
+  while (!open.empty()) {
+    std::vector<Range> nxt;
+    for (const Range& r : open) {
+      if (r.e - r.b <= kSahTask) {
+        tasks.push_back(r);
+        continue;
+      }
+      const size_t mid = B.split(r.node, r.b, r.e, true, r.depth);
+      uint32_t l, rr;
+      B.children(r.node, l, rr);
+      nxt.push_back({l, r.b, mid, r.depth + 1});
+      nxt.push_back({rr, mid, r.e, r.depth + 1});
+    }
+    open.swap(nxt);
+  }
+  std::sort(tasks.begin(), tasks.end(), [](const Range& a, const Range& b) { return a.e - a.b > b.e - b.b; });
+  std::atomic<size_t> ti{0};
+  const unsigned T = std::max(1u, host_threads());
+  std::vector<std::thread> th;
+  for (unsigned t = 0; t < T; ++t)
+    th.emplace_back([&] {
+      for (size_t k; (k = ti.fetch_add(1)) < tasks.size();)
+        B.build_serial(tasks[k].node, tasks[k].b, tasks[k].e, tasks[k].depth);
+    });
+  for (auto& x : th) x.join();
+}
+
 static void precompute_triangle(const RtTriangle64& T, float* r) {
   float v0x = T.v0[0], v0y = T.v0[1], v0z = T.v0[2];
   float ux = T.v1[0] - v0x, uy = T.v1[1] - v0y, uz = T.v1[2] - v0z;

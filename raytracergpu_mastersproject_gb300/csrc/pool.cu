@@ -506,12 +506,19 @@ rt_status rt_pool_add_scene(rt_pool* P, const RtSceneDesc* desc, uint32_t* out_i
     set_error("rt_pool_add_scene: " + msg);
     return RT_EINVAL;
   }
+  // The traversal tree, as in rt_scene_create_ex: a binned-SAH tree when the
+  // library builds in sorted mode on the host (the pool exports no S1 nodes,
+  // so none are built then), else the S1 array.
+  const bool use_sah = !desc->nodes && !(desc->build_flags & (RT_BUILD_ON_DEVICE | RT_BUILD_TRAVERSE_S1)) &&
+                       desc->bvh_mode == RT_BVH_SORTED && nt > 1;
   std::vector<RtBVHNode40> nodes;
   if (desc->nodes) {
     nodes.assign(desc->nodes, desc->nodes + (nt ? 2 * (size_t)nt - 1 : 0));
   } else if ((desc->build_flags & RT_BUILD_ON_DEVICE) && nt) {
     rt_status bs = device_build_to_host(wt.data(), nt, nullptr, 0, desc->bvh_mode, nodes);
     if (bs != RT_OK) return bs;
+  } else if (use_sah) {
+    build_sah(wt.data(), nt, nullptr, 0, nodes);
   } else {
     build_bvh(wt.data(), nt, nullptr, 0, desc->bvh_mode, nodes);
   }

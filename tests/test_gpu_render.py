@@ -279,3 +279,32 @@ def test_deep_stack_render_matches_per_pixel(rt, cuda):
         b = gpu_render(rt, cuda, s4, ubo, 64, 48, 3)
     assert np.array_equal(a, b)
     assert a[0::4].max() > 0.1
+
+
+def test_stream_release_frees_and_recreates_workspace(rt, cuda):
+    """rt_stream_release drops the stream's workspace (including the path
+    tracer's scratch); the next call on the stream allocates a new one and
+    renders the same frame."""
+    tris, mats = lit_scene(rt)
+    ubo = rt.make_ubo((0.0, 0.5, 4.0), (0.0, 0.0, 0.0), fov=60.0, depth=4, random_state=21)
+    st = cuda.cuda.Stream()
+    w, h = 80, 45
+
+    def frame(sc):
+        acc = cuda.empty(w * h * 4, dtype=cuda.float32, device="cuda")
+        cuda.cuda.synchronize()
+        rt.accum_clear(acc, w, h, stream=st)
+        sc.render(ubo, acc, w, h, 4, stream=st)
+        st.synchronize()
+        return acc.cpu().numpy()
+
+    with rt.Scene(tris, materials=mats) as sc:
+        a = frame(sc)
+        free0 = cuda.cuda.mem_get_info()[0]
+        rt.release_stream(st)
+        free1 = cuda.cuda.mem_get_info()[0]
+        b = frame(sc)
+        rt.release_stream(st)
+        rt.release_stream(st)  # nothing left to free
+    assert np.array_equal(a, b)
+    assert free1 >= free0
