@@ -518,8 +518,9 @@ def run_ours(args):
         barrier()
         e2e = {"value": n * ws / (dt / k) / 1e9, "unit": UNIT, "h2d_bytes_per_step": n * 32,
                "d2h_bytes_per_step": n * 8, "steps": k, "ms_per_step": dt / k * 1e3,
-               "path": "rt_trace_host, pinned host buffers; chunks of 512 Ki, 2 Mi, 8 Mi... rays alternate over two "
-                       "trace streams while copy-in and copy-out overlap the tracing"}
+               "path": "rt_trace_host, pinned host buffers: rays staged in chunks of 512 Ki, 4 Mi, then the rest, "
+                       "uploaded on a copy stream while the previous chunk traces (two trace streams); the kernels "
+                       "write hits straight into the pinned host buffer"}
         hits_dev = d_hits.cpu().numpy().view(rt.HIT_DTYPE)
         assert np.array_equal(hits_dev.view(np.uint64), hh.view(np.uint64)), "e2e hits differ from device hits"
     clocks.stop()

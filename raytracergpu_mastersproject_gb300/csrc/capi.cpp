@@ -503,26 +503,36 @@ rt_status rt_trace_host(rt_scene* scene, const RtRay* h_rays, uint32_t n, RtHit*
   Workspace* w = nullptr;
   rt_status s = workspace(st, &w);
   if (s != RT_OK) return s;
-  // Chunks alternate between two buffers and two trace streams (the caller's
-  // and trace2), each with its own counters and reorder scratch; copy-in and
-  // copy-out run on streams of their own, so chunk i+1 uploads and chunk i-1
-  // downloads while chunk i traces, and chunk i+1's blocks take the SMs that
-  // chunk i's last rays leave idle.  Every launch still ends with a drain of
-  // its in-flight rays at falling SIMT efficiency, so chunks are few and
-  // large: the first is small (its upload is not overlapped) and each next
-  // one 4x larger, up to the buffer size.
-  static const uint32_t kMaxChunk = [] {
-    const char* e = std::getenv("RT_HOST_CHUNK_RAYS");
-    const long v = e ? std::atol(e) : 0;
-    return v >= 4096 && v <= (1l << 30) ? (uint32_t)v : (1u << 23);
-  }();
+  // Chunks alternate between two ray buffers and two trace streams (the
+  // caller's and trace2), each with its own counters and reorder scratch;
+  // copy-in runs on a stream of its own, so chunk i+1 uploads while chunk i
+  // traces, and chunk i+1's blocks take the SMs that chunk i's last rays
+  // leave idle.  Every launch still ends with a drain of its in-flight rays at
+  // falling SIMT efficiency, so chunks are few and large: the first is small
+  // (its upload is not overlapped) and each next one several times larger.
+  //
+  // Hits: when h_hits is page-locked host memory the kernels write them
+  // there directly over the host link (scattered 8-byte stores, overlapped
+  // with tracing), so nothing is downloaded at the end and chunks grow 8x;
+  // otherwise they are staged in device memory and downloaded per chunk on a
+  // third stream, and chunks grow 4x (a smaller last chunk to download).
   static const uint32_t kFirstChunk = [] {
     const char* e = std::getenv("RT_HOST_FIRST_CHUNK_RAYS");
     const long v = e ? std::atol(e) : 0;
     return v >= 4096 && v <= (1l << 30) ? (uint32_t)v : (1u << 19);
   }();
-  const uint32_t chunk = std::min<uint32_t>(n, kMaxChunk);  // buffer capacity
-  const size_t per = (size_t)chunk * (sizeof(RtRay) + sizeof(RtHit));
+  RtHit* direct = nullptr;
+  {
+    cudaPointerAttributes pa;
+    if (cudaPointerGetAttributes(&pa, h_hits) == cudaSuccess && pa.type == cudaMemoryTypeHost && pa.devicePointer)
+      direct = static_cast<RtHit*>(pa.devicePointer);
+    else
+      cudaGetLastError();  // an unregistered pointer is not an error here
+  }
+  const uint32_t growth = direct ? 8u : 4u;
+  const uint32_t chunk = std::min<uint32_t>(n, direct ? (1u << 24) : (1u << 23));  // buffer capacity
+  const size_t ray_bytes = (size_t)chunk * sizeof(RtRay), hit_bytes = direct ? 0 : (size_t)chunk * sizeof(RtHit);
+  const size_t per = ray_bytes + hit_bytes;
   const size_t need = 2 * per;
   cudaError_t e;
   if (w->stage_bytes < need) {
@@ -547,23 +557,25 @@ rt_status rt_trace_host(rt_scene* scene, const RtRay* h_rays, uint32_t n, RtHit*
   }
   char* base = static_cast<char*>(w->stage);
   RtRay* drays[2] = {reinterpret_cast<RtRay*>(base), reinterpret_cast<RtRay*>(base + per)};
-  RtHit* dhits[2] = {reinterpret_cast<RtHit*>(base + (size_t)chunk * sizeof(RtRay)),
-                     reinterpret_cast<RtHit*>(base + per + (size_t)chunk * sizeof(RtRay))};
+  RtHit* dhits[2] = {reinterpret_cast<RtHit*>(base + ray_bytes), reinterpret_cast<RtHit*>(base + per + ray_bytes)};
   cudaStream_t tst[2] = {st, w->trace2};
   uint32_t* counters[2] = {w->counters, w->counters + 4};
   cudaEvent_t* in_done = &w->ev[0];
   cudaEvent_t* trace_done = &w->ev[2];
   cudaEvent_t* out_done = &w->ev[4];
+  // buffers b are free again once chunk c-2 is traced (direct) or downloaded
+  cudaEvent_t* free_again = direct ? trace_done : out_done;
   // the caller's earlier work on `stream` comes first (trace2 follows it
   // through copy_in's events)
   if ((e = cudaEventRecord(w->ev[6], st)) != cudaSuccess) return cuda_fail(e, "event");
   if ((e = cudaStreamWaitEvent(w->copy_in, w->ev[6], 0)) != cudaSuccess) return cuda_fail(e, "wait");
-  uint32_t size = std::min(chunk, kFirstChunk);
-  for (uint32_t c = 0, off = 0, cnt = 0; off < n; ++c, off += cnt, size = (uint32_t)std::min<uint64_t>(4ull * size, chunk)) {
+  uint32_t size = std::min(chunk, kFirstChunk), chunks = 0;
+  for (uint32_t c = 0, off = 0, cnt = 0; off < n;
+       ++c, off += cnt, size = (uint32_t)std::min<uint64_t>((uint64_t)growth * size, chunk)) {
     const uint32_t b = c & 1u;
     cnt = std::min(size, n - off);
-    // buffers b are free once chunk c-2 has been downloaded
-    if (c >= 2 && (e = cudaStreamWaitEvent(w->copy_in, out_done[b], 0)) != cudaSuccess) return cuda_fail(e, "wait");
+    chunks = c + 1;
+    if (c >= 2 && (e = cudaStreamWaitEvent(w->copy_in, free_again[b], 0)) != cudaSuccess) return cuda_fail(e, "wait");
     if ((e = cudaMemcpyAsync(drays[b], h_rays + off, (size_t)cnt * sizeof(RtRay), cudaMemcpyHostToDevice,
                              w->copy_in)) != cudaSuccess)
       return cuda_fail(e, "rt_trace_host: H2D");
@@ -572,14 +584,23 @@ rt_status rt_trace_host(rt_scene* scene, const RtRay* h_rays, uint32_t n, RtHit*
     uint32_t* order = nullptr;
     if ((s = maybe_reorder(w, scene->d, drays[b], cnt, flags, tst[b], &order, b * slot)) != RT_OK) return s;
     if ((e = cudaMemsetAsync(counters[b], 0, 2 * sizeof(uint32_t), tst[b])) != cudaSuccess) return cuda_fail(e, "memset");
-    if ((e = launch_trace(scene->d, drays[b], cnt, dhits[b], flags, counters[b], tst[b], order)) != cudaSuccess)
+    RtHit* out = direct ? direct + off : dhits[b];
+    if ((e = launch_trace(scene->d, drays[b], cnt, out, flags, counters[b], tst[b], order)) != cudaSuccess)
       return cuda_fail(e, "rt_trace_host: launch");
     if ((e = cudaEventRecord(trace_done[b], tst[b])) != cudaSuccess) return cuda_fail(e, "event");
+    if (direct) continue;
     if ((e = cudaStreamWaitEvent(w->copy_out, trace_done[b], 0)) != cudaSuccess) return cuda_fail(e, "wait");
     if ((e = cudaMemcpyAsync(h_hits + off, dhits[b], (size_t)cnt * sizeof(RtHit), cudaMemcpyDeviceToHost,
                              w->copy_out)) != cudaSuccess)
       return cuda_fail(e, "rt_trace_host: D2H");
     if ((e = cudaEventRecord(out_done[b], w->copy_out)) != cudaSuccess) return cuda_fail(e, "event");
+  }
+  if (direct) {
+    // the caller's stream continues after trace2's last chunk; its own chunks
+    // are already in order on it
+    if (chunks >= 2 && (e = cudaStreamWaitEvent(st, trace_done[1], 0)) != cudaSuccess) return cuda_fail(e, "wait");
+    if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return cuda_fail(e, "rt_trace_host: sync");
+    return RT_OK;
   }
   // the caller's stream continues after the last download (every chunk's
   // download waited for its trace, so trace2 is drained too)

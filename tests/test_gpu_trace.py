@@ -120,10 +120,18 @@ def test_trace_host_matches_device(rt, cuda):
         d = sc.trace_host(pinned.numpy().view(rt.RAY_DTYPE), sort=True)
         e = sc.trace_host(pinned.numpy().view(rt.RAY_DTYPE), any_hit=True)
         f = dev_trace(rt, cuda, sc, rays, any_hit=True)
+        # page-locked hits: the kernels write them directly (chunks of 512 Ki, 4 Mi and the rest)
+        out_t = cuda.full((len(rays) * 8,), 0xCD, dtype=cuda.uint8).pin_memory()
+        out = out_t.numpy().view(rt.HIT_DTYPE)
+        g = sc.trace_host(pinned.numpy().view(rt.RAY_DTYPE), out=out, sort=True).copy()
+        out_t.fill_(0xCD)
+        h = sc.trace_host(rays, out=out, any_hit=True).copy()
     assert np.array_equal(a.view(np.uint64), b.view(np.uint64))
     assert np.array_equal(a.view(np.uint64), c.view(np.uint64))
     assert np.array_equal(a.view(np.uint64), d.view(np.uint64))
     assert np.array_equal(e.view(np.uint64), f.view(np.uint64))
+    assert np.array_equal(a.view(np.uint64), g.view(np.uint64))
+    assert np.array_equal(f.view(np.uint64), h.view(np.uint64))
 
 
 def test_caller_supplied_nodes(rt, orc, cuda):
