@@ -395,3 +395,31 @@ def test_deep_stacks_spill_the_shared_ring(rt, orc, cuda):
     assert np.array_equal(closest4.view(np.uint64), sorted4.view(np.uint64))
     hit = ref["prim"] != orc.NO_HIT
     assert np.array_equal(any4["prim"] != orc.NO_HIT, hit)  # any-hit finds a hit exactly where one exists
+
+
+def _t64_errors(orc, tris, rays, hits):
+    i = np.nonzero(hits["prim"] != orc.NO_HIT)[0]
+    t64 = np.array([orc.triangle_t64(tris[hits["prim"][k]], rays[k])[0] for k in i])
+    return i, t64, np.abs(hits["t"][i].astype(np.float64) - t64)
+
+
+def test_hit_t_against_fp64(rt, orc, cuda):
+    """Hit t against the same triangle intersected in binary64.  Config 1:
+    within 1e-5 relative on every hit.  A config-3 soup: the reference's
+    binary32 plane test, D - dot(n, o), cancels for short hits, so the bound
+    there is 1e-5 of max(t, scene extent 1); the kernels return the
+    reference's binary32 t bit for bit either way."""
+    tris, ubo, rays = rt.gen_config1()
+    with rt.Scene(tris) as sc:
+        got = dev_trace(rt, cuda, sc, rays[::2])
+    i, t64, err = _t64_errors(orc, tris, rays[::2], got)
+    assert len(i) > 50_000
+    assert np.all(err <= 1e-5 * np.abs(t64))
+
+    from raytracergpu_mastersproject_gb300 import workloads as W
+    tris3, rays3 = W.config3(262_144, 50_000)
+    with rt.Scene(tris3) as sc:
+        got3 = dev_trace(rt, cuda, sc, rays3)
+    i3, t3, err3 = _t64_errors(orc, tris3, rays3, got3)
+    assert len(i3) > 10_000
+    assert np.all(err3 <= 1e-5 * np.maximum(np.abs(t3), 1.0))
