@@ -115,9 +115,11 @@ __global__ void __launch_bounds__(THREADS, MINB)
     }
     if (local == 0xFFFFFFFFu) continue;
     bool done = false;
+    // a node visit, then in the same iteration the leaf it led to
     if (dev::is_inner(s.node)) {
       if (!dev::visit_wide_stk<STACK>(S, s, stk)) done = true;
-    } else if (dev::is_leaf(s.node)) {
+    }
+    if (!done && dev::is_leaf(s.node)) {
       if (dev::leaf_visit<ANY>(S, s, s.node))
         done = true;
       else

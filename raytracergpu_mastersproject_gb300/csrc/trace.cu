@@ -101,9 +101,12 @@ __global__ void __launch_bounds__(THREADS, MINB)
 }
 
 // Per-step variant for 4-wide trees: every iteration each lane advances its
-// ray by exactly one step -- one inner node, or one leaf -- and lanes whose ray
-// finished take new rays as soon as `refill` of them are idle.  The heavy
-// inner-node step then runs with nearly all lanes active; leaves are rare.
+// ray by one step -- one inner node, then the leaf that node led to if any,
+// or one leaf -- and lanes whose ray finished take new rays as soon as
+// `refill` of them are idle.  The heavy inner-node step then runs with nearly
+// all lanes active.  Some lane needs the leaf code in nearly every iteration,
+// so a lane that reaches a leaf tests it at once instead of in an iteration
+// of its own (config 3: 14.2 -> 13.4 ms).
 //
 // RAW (the path tracer's queries): n == 0xFFFFFFFF reads the ray count from
 // counter[2], written by the kernel that produced the rays; each hit is the
@@ -159,9 +162,12 @@ __global__ void __launch_bounds__(THREADS, MINB)
     }
     if (ray == 0xFFFFFFFFu) continue;
     bool done = false;
+    // a node visit, then in the same iteration the leaf it led to (the warp
+    // runs the leaf code in nearly every iteration for some lane anyway)
     if (dev::is_inner(s.node)) {
       if (!dev::visit_wide_stk<STACK>(S, s, stk)) done = true;
-    } else if (dev::is_leaf(s.node)) {
+    }
+    if (!done && dev::is_leaf(s.node)) {
       if (dev::leaf_visit<ANY>(S, s, s.node))
         done = true;
       else
