@@ -259,6 +259,11 @@ Variant make_variant() {
   return v;
 }
 
+// Launch shapes (RT_TRACE_VARIANT selects one; RT_TRACE_REFILL sets the refill
+// threshold): 0-2 while-while loop at 12 / 10 / 1 blocks per SM, 3-5 step
+// loop with the stack in local memory, 6 (default) step loop at 10 blocks of
+// 128 threads with a 16-entry shared ring, 7 the same as 5 blocks of 256.
+// Binary trees always use the while-while loop of the chosen shape.
 Variant g_variants[] = {make_variant<128, 12, false>(), make_variant<128, 10, false>(), make_variant<128, 1, false>(),
                         make_variant<128, 12, true>(),  make_variant<128, 10, true>(),  make_variant<128, 1, true>(),
                         make_variant<128, 10, true, 16>(), make_variant<256, 5, true, 16>()};
