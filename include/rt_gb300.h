@@ -476,6 +476,15 @@ const char* rt_last_error_string(void);
 uint32_t rt_abi_version(void);
 /* Waits for the stream with a deadline; RT_ETIMEOUT when it runs out. */
 rt_status rt_stream_wait(void* stream, double timeout_seconds);
+/* Device-side index checks (no counterpart in the reference).  A library
+ * built with RT_DEVICE_CHECKS=1 (librt_gb300_checked.so) checks every node,
+ * primitive, ray, material and path index its kernels use against the
+ * scene's arrays; an index out of range sets a bit in the scene's check word
+ * (1 node, 2 triangle, 4 sphere, 8 ray, 16 material, 32 path), records the
+ * first bad index, and the access is skipped.  rt_scene_device_checks reads
+ * and clears the word (synchronous; always 0 in the normal build). */
+uint32_t rt_device_checks_compiled(void);
+rt_status rt_scene_device_checks(rt_scene* scene, uint32_t* bits, uint32_t* first_index);
 /* Frees the device workspace the library keeps for this stream on the current
  * device (work counters, ray staging, reorder and path-tracing scratch), after
  * the stream's work has finished.  No call on the stream may run concurrently;

@@ -153,6 +153,8 @@ SIGNATURES = {
     "rt_last_error_string": (C.c_char_p, []),
     "rt_abi_version": (_U32, []),
     "rt_stream_wait": (_I, [_P, _D]),
+    "rt_device_checks_compiled": (_U32, []),
+    "rt_scene_device_checks": (_I, [_P, C.POINTER(_U32), C.POINTER(_U32)]),
     "rt_stream_release": (_I, [_P]),
     "rt_pool_create": (_I, [C.POINTER(PoolOptions), C.POINTER(C.c_void_p)]),
     "rt_pool_destroy": (_I, [_P]),
@@ -337,6 +339,12 @@ class Scene:
         _check(lib().rt_render_count(self.handle, C.byref(ubo), _ptr(accum), width, height, spp, C.byref(opt),
                                      _stream_handle(stream), c), "rt_render_count")
         return int(c[0]), int(c[1]), int(c[2])
+
+    def device_checks(self) -> tuple[int, int]:
+        """Reads and clears the checked build's index-check word -> (bits, first bad index)."""
+        b, f = C.c_uint32(), C.c_uint32()
+        _check(lib().rt_scene_device_checks(self.handle, C.byref(b), C.byref(f)), "rt_scene_device_checks")
+        return b.value, f.value
 
     def close(self) -> None:
         if getattr(self, "_h", None) is not None and self._h.value:
@@ -546,6 +554,11 @@ class Server:
 
     def __exit__(self, *a):
         self.close()
+
+
+def device_checks_compiled() -> bool:
+    """True for the checked build (RT_DEVICE_CHECKS=1)."""
+    return bool(lib().rt_device_checks_compiled())
 
 
 def release_stream(stream=None) -> None:

@@ -19,6 +19,9 @@ CSRC = PKG / "csrc"
 INCLUDE = PKG.parent / "include"
 BUILD = PKG / "_build"
 LIB = PKG / "librt_gb300.so"
+# The checked build: device-side index checks (RT_DEVICE_CHECKS=1).
+BUILD_CHECKED = PKG / "_build_checked"
+LIB_CHECKED = PKG / "librt_gb300_checked.so"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-std=c++17", "-lineinfo", "-fmad=false", "--expt-relaxed-constexpr",
@@ -44,18 +47,21 @@ def _stale(lib: Path, deps: list[Path]) -> bool:
     return any(d.stat().st_mtime > t for d in deps)
 
 
-def build(force: bool = False, verbose: bool = False, extra_flags: list[str] | None = None) -> Path:
-    """Compiles and links librt_gb300.so; returns its path."""
+def build(force: bool = False, verbose: bool = False, extra_flags: list[str] | None = None,
+          checked: bool = False) -> Path:
+    """Compiles and links librt_gb300.so (librt_gb300_checked.so with the
+    device-side index checks when `checked`); returns its path."""
+    lib_path, bdir = (LIB_CHECKED, BUILD_CHECKED) if checked else (LIB, BUILD)
     srcs = sources()
     deps = srcs + list(CSRC.glob("*.h")) + list(CSRC.glob("*.cuh")) + list(INCLUDE.glob("*.h")) + [Path(__file__)]
-    if not force and not _stale(LIB, deps):
-        return LIB
-    BUILD.mkdir(exist_ok=True)
+    if not force and not _stale(lib_path, deps):
+        return lib_path
+    bdir.mkdir(exist_ok=True)
     cc = nvcc()
-    flags = COMMON + ARCH + list(extra_flags or [])
+    flags = COMMON + ARCH + list(extra_flags or []) + (["-DRT_DEVICE_CHECKS=1"] if checked else [])
 
     def compile_one(src: Path) -> Path:
-        obj = BUILD / (src.name + ".o")
+        obj = bdir / (src.name + ".o")
         cmd = [cc, *flags, "-c", str(src), "-o", str(obj)]
         if verbose:
             print(" ".join(cmd), flush=True)
@@ -68,16 +74,16 @@ def build(force: bool = False, verbose: bool = False, extra_flags: list[str] | N
 
     with cf.ThreadPoolExecutor(max_workers=min(len(srcs), os.cpu_count() or 4)) as ex:
         objs = list(ex.map(compile_one, srcs))
-    tmp = LIB.with_suffix(".so.tmp")
+    tmp = lib_path.with_suffix(".so.tmp")
     cmd = [cc, "-shared", *ARCH, "-Xcompiler", "-pthread", "-o", str(tmp), *map(str, objs)]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
-    os.replace(tmp, LIB)
-    return LIB
+    os.replace(tmp, lib_path)
+    return lib_path
 
 
 if __name__ == "__main__":
     import sys
 
-    print(build(force="--force" in sys.argv, verbose="-v" in sys.argv))
+    print(build(force="--force" in sys.argv, verbose="-v" in sys.argv, checked="--checked" in sys.argv))

@@ -17,6 +17,10 @@
 
 #include "rt_internal.h"
 
+#ifndef RT_DEVICE_CHECKS
+#define RT_DEVICE_CHECKS 0
+#endif
+
 struct rt_scene {
   rtgb::DeviceScene d;
   void* mem = nullptr;
@@ -179,6 +183,22 @@ rt_status rt_stream_wait(void* stream, double timeout_seconds) {
     }
     std::this_thread::sleep_for(std::chrono::microseconds(50));
   }
+}
+
+uint32_t rt_device_checks_compiled(void) { return RT_DEVICE_CHECKS; }
+
+rt_status rt_scene_device_checks(rt_scene* scene, uint32_t* bits, uint32_t* first_index) {
+  if (!scene || !bits) {
+    set_error("rt_scene_device_checks: bad argument");
+    return RT_EINVAL;
+  }
+  uint32_t w[2] = {0, 0};
+  cudaError_t e = cudaMemcpy(w, scene->d.check, sizeof(w), cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemset(scene->d.check, 0, sizeof(w));
+  if (e != cudaSuccess) return cuda_fail(e, "rt_scene_device_checks");
+  *bits = w[0];
+  if (first_index) *first_index = w[1] & 0x7FFFFFFFu;
+  return RT_OK;
 }
 
 rt_status rt_stream_release(void* stream) {
@@ -360,6 +380,8 @@ rt_status rt_scene_create_ex(const RtSceneDesc* desc, rt_scene** out_scene) {
   sc->d.tri_mat = static_cast<const uint32_t*>(put(hb.tri_mat.data(), b_mat));
   sc->d.spheres = put(hb.spheres.data(), b_sph);
   sc->d.mats = put(hb.mats.data(), b_mats);
+  sc->d.check = reinterpret_cast<uint32_t*>(p);  // the trailing 256 bytes
+  if (e == cudaSuccess) e = cudaMemset(p, 0, 8);
   if (e != cudaSuccess) {
     cudaFree(sc->mem);
     sc->mem = nullptr;

@@ -104,6 +104,9 @@ __device__ __forceinline__ bool bounce(const DeviceScene& S, const dev::Trav& s,
   const float t = s.tclose;
   f3 p, n;
   uint32_t mat;
+  if (dev::chk(S.check, (s.best & kSphereBit) ? (s.best & kSphereMask) >= S.n_spheres : (s.best & kSlotMask) >= S.n_tris,
+               (s.best & kSphereBit) ? dev::kChkSphere : dev::kChkTri, s.best))
+    return false;
   if (s.best & kSphereBit) {
     const uint32_t idx = s.best & kSphereMask;
     const float4 c0 = dev::ldg4(S.spheres, 2u * idx);
@@ -118,6 +121,7 @@ __device__ __forceinline__ bool bounce(const DeviceScene& S, const dev::Trav& s,
     n = mk(r0.x, r0.y, r0.z);
     mat = __ldg(&S.tri_mat[slot]);
   }
+  if (dev::chk(S.check, mat >= S.n_mats, dev::kChkMat, mat)) return false;
   const int back = dot(cd, n) > 0.0f ? 1 : 0;
   n = scale(n, (float)(1 - 2 * back));
   const float4 m0 = dev::ldg4(S.mats, 2u * mat);
@@ -466,7 +470,7 @@ __global__ void k_wave_shade(DeviceScene S, uint32_t level, uint32_t depth, uint
     bool more = false;
     uint32_t p = 0;
     f3 co = mk(0.0f, 0.0f, 0.0f), cd = co;
-    if (i < n) {
+    if (i < n && !dev::chk(S.check, level > 0 && list[i] >= n0, dev::kChkPath, level > 0 ? list[i] : i)) {
       p = level == 0 ? i : list[i];
       const uint32_t r = level == 0 ? (per_path ? i : i / ns) : i;
       const float4 o = rays[2 * (size_t)r], d = rays[2 * (size_t)r + 1];

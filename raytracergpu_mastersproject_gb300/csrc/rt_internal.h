@@ -70,6 +70,9 @@ struct DeviceScene {
   uint32_t width = 2;       // 2: binary child-box nodes; 4: quantised 4-wide nodes
   uint32_t stack_need = 0;  // worst-case traversal stack entries
   float box[6] = {0, 0, 0, 0, 0, 0};  // root box: lo xyz, hi xyz
+  // Checked builds (RT_DEVICE_CHECKS=1): word 0 collects the kChk* bits of
+  // out-of-range indices, word 1 the first bad index | 2^31.  May be null.
+  uint32_t* check = nullptr;
 };
 
 // Host-side result of the BVH conversion, ready to upload.

@@ -55,8 +55,12 @@ __global__ void __launch_bounds__(THREADS, MINB)
         const uint32_t id = base + (uint32_t)__popc(m & lanemask_lt());
         if (id < n) {
           ray = order ? __ldg(&order[id]) : id;
-          dev::trav_init_ray(s, __ldg(&rays[2u * ray]), __ldg(&rays[2u * ray + 1u]), S.root);
-          if constexpr (W == 2) stack[0] = kSentinel;
+          if (dev::chk(S.check, ray >= n, dev::kChkRay, ray)) {
+            ray = 0xFFFFFFFFu;
+          } else {
+            dev::trav_init_ray(s, __ldg(&rays[2u * ray]), __ldg(&rays[2u * ray + 1u]), S.root);
+            if constexpr (W == 2) stack[0] = kSentinel;
+          }
         }
       }
     }
@@ -149,7 +153,7 @@ __global__ void __launch_bounds__(THREADS, MINB)
       if (base + (uint32_t)__popc(idle) >= n) exhausted = true;
       if (ray == 0xFFFFFFFFu) {
         const uint32_t id = base + (uint32_t)__popc(idle & lanemask_lt());
-        if (id < n) {
+        if (id < n && !dev::chk(S.check, order && __ldg(&order[id]) >= n, dev::kChkRay, order ? __ldg(&order[id]) : id)) {
           ray = order ? __ldg(&order[id]) : id;
           dev::trav_init_ray(s, __ldg(&rays[2u * ray]), __ldg(&rays[2u * ray + 1u]), S.root);
           stk.reset();

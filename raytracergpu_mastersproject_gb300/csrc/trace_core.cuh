@@ -74,6 +74,27 @@ __device__ __forceinline__ bool sphere_test(const void* spheres, uint32_t idx, f
 
 // ---------------------------------------------------------- traversal ----
 // One ray's traversal state; kept in registers across warp refills.
+#ifndef RT_DEVICE_CHECKS
+#define RT_DEVICE_CHECKS 0
+#endif
+// Device-side index checks of the checked build (RT_DEVICE_CHECKS=1), in
+// place of a sanitizer: an index outside its array sets a bit in the scene's
+// check word, records the first bad index, and the access is skipped (the
+// ray ends as a miss).  In the normal build chk() is constant false.
+enum : uint32_t { kChkNode = 1u, kChkTri = 2u, kChkSphere = 4u, kChkRay = 8u, kChkMat = 16u, kChkPath = 32u };
+__device__ __forceinline__ bool chk(uint32_t* word, bool bad, uint32_t bit, uint32_t value) {
+#if RT_DEVICE_CHECKS
+  if (bad && word) {
+    atomicOr(word, bit);
+    atomicCAS(word + 1, 0u, value | 0x80000000u);
+  }
+  return bad;
+#else
+  (void)word; (void)bad; (void)bit; (void)value;
+  return false;
+#endif
+}
+
 struct Trav {
   float ox, oy, oz, dx, dy, dz;  // the ray exactly as given (triangle tests)
   float ix, iy, iz;              // 1/d, with zero components replaced
@@ -150,6 +171,7 @@ template <bool ANY>
 __device__ __forceinline__ bool leaf_visit(const DeviceScene& S, Trav& s, uint32_t leaf) {
   if (leaf & kSphereBit) {
     const uint32_t idx = leaf & kSphereMask;
+    if (chk(S.check, idx >= S.n_spheres, kChkSphere, idx)) return false;
     float t;
     s.ntest++;
     if (idx < S.n_spheres && sphere_test(S.spheres, idx, s.ox, s.oy, s.oz, s.dx, s.dy, s.dz, s.tmin, s.tclose, t)) {
@@ -161,6 +183,7 @@ __device__ __forceinline__ bool leaf_visit(const DeviceScene& S, Trav& s, uint32
   }
   const uint32_t first = leaf & kSlotMask;
   const uint32_t count = ((leaf >> kCountShift) & 7u) + 1u;
+  if (chk(S.check, first + count > S.n_tris, kChkTri, first)) return false;
   for (uint32_t k = 0; k < count; ++k) {
     float t;
     s.ntest++;
@@ -182,6 +205,10 @@ __device__ __forceinline__ bool trav_run(const DeviceScene& S, Trav& s, uint32_t
   for (;;) {
     // Inner nodes: descend, postponing the first leaf found.
     while (is_inner(s.node)) {
+      if (chk(S.check, s.node >= S.n_inner, kChkNode, s.node)) {
+        s.sp = -1;
+        return false;
+      }
       s.nvis++;
       const float4 a = ldg4(S.inner, 4u * s.node + 0u);
       const float4 b = ldg4(S.inner, 4u * s.node + 1u);
@@ -337,6 +364,10 @@ __device__ __forceinline__ float qbyte(uint32_t w) {
 // overflow (s.sp = -1).
 template <int STACK, class Stk>
 __device__ __forceinline__ bool visit_wide_stk(const DeviceScene& S, Trav& s, Stk& stk) {
+  if (chk(S.check, s.node >= S.n_inner, kChkNode, s.node)) {
+    s.sp = -1;  // ends the ray like a stack overflow
+    return false;
+  }
   s.nvis++;
   const float4 h = ldg4(S.inner, 4u * s.node + 0u);
   const float4 r = ldg4(S.inner, 4u * s.node + 1u);
