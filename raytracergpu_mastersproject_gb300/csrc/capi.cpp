@@ -233,6 +233,7 @@ rt_status rt_stream_release(void* stream) {
 rt_status rt_build_bvh(const RtTriangle64* triangles, uint32_t num_triangles, const RtSphere32* spheres,
                        uint32_t num_spheres, const RtModel64* models, uint32_t num_models, uint32_t bvh_mode,
                        RtBVHNode40* out_nodes) {
+  rtgb::NvtxRange nvtx_range("rt_build_bvh");
   const uint64_t N = (uint64_t)num_triangles + num_spheres;
   if ((num_triangles && !triangles) || (num_spheres && !spheres) || (N && !out_nodes) ||
       (bvh_mode != RT_BVH_SORTED && bvh_mode != RT_BVH_REFERENCE) || N > kMaxTriangles) {
@@ -255,6 +256,7 @@ rt_status rt_build_bvh(const RtTriangle64* triangles, uint32_t num_triangles, co
 rt_status rt_build_bvh_sah(const RtTriangle64* triangles, uint32_t num_triangles, const RtSphere32* spheres,
                            uint32_t num_spheres, const RtModel64* models, uint32_t num_models,
                            RtBVHNode40* out_nodes) {
+  rtgb::NvtxRange nvtx_range("rt_build_bvh_sah");
   const uint64_t N = (uint64_t)num_triangles + num_spheres;
   if ((num_triangles && !triangles) || (num_spheres && !spheres) || (N && !out_nodes) || N > kMaxTriangles) {
     set_error("rt_build_bvh_sah: bad argument");
@@ -274,6 +276,7 @@ rt_status rt_build_bvh_sah(const RtTriangle64* triangles, uint32_t num_triangles
 }
 
 rt_status rt_scene_create_ex(const RtSceneDesc* desc, rt_scene** out_scene) {
+  rtgb::NvtxRange nvtx_range("rt_scene_create_ex");
   if (!desc || !out_scene) {
     set_error("rt_scene_create_ex: null argument");
     return RT_EINVAL;
@@ -467,6 +470,7 @@ rt_status rt_scene_get_nodes(const rt_scene* scene, RtBVHNode40* h_out, uint32_t
 }
 
 rt_status rt_trace(rt_scene* scene, const RtRay* d_rays, uint32_t n, RtHit* d_hits, uint32_t flags, void* stream) {
+  rtgb::NvtxRange nvtx_range("rt_trace");
   if (!scene || (n && (!d_rays || !d_hits)) || flags > (RT_TRACE_ANY | RT_TRACE_SORT) || n > 0x80000000u) {
     set_error("rt_trace: bad argument");
     return RT_EINVAL;
@@ -487,6 +491,7 @@ rt_status rt_trace(rt_scene* scene, const RtRay* d_rays, uint32_t n, RtHit* d_hi
 
 rt_status rt_trace_count(rt_scene* scene, const RtRay* d_rays, uint32_t n, RtHit* d_hits, uint32_t flags,
                          void* stream, uint64_t* h_counts) {
+  rtgb::NvtxRange nvtx_range("rt_trace_count");
   if (!scene || !h_counts || (n && (!d_rays || !d_hits)) || flags > (RT_TRACE_ANY | RT_TRACE_SORT) ||
       n > 0x80000000u) {
     set_error("rt_trace_count: bad argument");
@@ -516,6 +521,7 @@ rt_status rt_trace_count(rt_scene* scene, const RtRay* d_rays, uint32_t n, RtHit
 
 rt_status rt_trace_host(rt_scene* scene, const RtRay* h_rays, uint32_t n, RtHit* h_hits, uint32_t flags,
                         void* stream) {
+  rtgb::NvtxRange nvtx_range("rt_trace_host");
   if (!scene || (n && (!h_rays || !h_hits)) || flags > (RT_TRACE_ANY | RT_TRACE_SORT) || n > 0x80000000u) {
     set_error("rt_trace_host: bad argument");
     return RT_EINVAL;
@@ -705,11 +711,13 @@ static rt_status render_impl(rt_scene* scene, const RtRaytraceUBO* ubo, float* d
 
 rt_status rt_render(rt_scene* scene, const RtRaytraceUBO* ubo, float* d_accum, uint32_t width, uint32_t height,
                     uint32_t spp, const RtRenderOptions* opt, void* stream) {
+  rtgb::NvtxRange nvtx_range("rt_render");
   return render_impl(scene, ubo, d_accum, width, height, spp, opt, stream, nullptr, "rt_render");
 }
 
 rt_status rt_render_count(rt_scene* scene, const RtRaytraceUBO* ubo, float* d_accum, uint32_t width, uint32_t height,
                           uint32_t spp, const RtRenderOptions* opt, void* stream, uint64_t* h_counts) {
+  rtgb::NvtxRange nvtx_range("rt_render_count");
   if (!h_counts) {
     set_error("rt_render_count: bad argument");
     return RT_EINVAL;
@@ -718,6 +726,7 @@ rt_status rt_render_count(rt_scene* scene, const RtRaytraceUBO* ubo, float* d_ac
 }
 
 rt_status rt_accum_clear(float* d_accum, uint32_t width, uint32_t height, void* stream) {
+  rtgb::NvtxRange nvtx_range("rt_accum_clear");
   if (!d_accum || (uint64_t)width * height > 0x40000000ull) {
     set_error("rt_accum_clear: bad argument");
     return RT_EINVAL;
@@ -727,6 +736,7 @@ rt_status rt_accum_clear(float* d_accum, uint32_t width, uint32_t height, void* 
 }
 
 rt_status rt_resolve(const float* d_accum, uint32_t width, uint32_t height, uint32_t spp, float* d_out, void* stream) {
+  rtgb::NvtxRange nvtx_range("rt_resolve");
   if (!d_accum || !d_out || spp == 0 || (uint64_t)width * height > 0x40000000ull) {
     set_error("rt_resolve: bad argument");
     return RT_EINVAL;

@@ -479,6 +479,7 @@ rt_status rt_pool_destroy(rt_pool* P) {
 }
 
 rt_status rt_pool_add_scene(rt_pool* P, const RtSceneDesc* desc, uint32_t* out_id) {
+  NvtxRange nvtx_range("rt_pool_add_scene");
   if (!P || !desc || !out_id) {
     set_error("rt_pool_add_scene: null argument");
     return RT_EINVAL;
@@ -657,6 +658,7 @@ rt_status rt_pool_get_info(const rt_pool* Pc, RtPoolInfo* out) {
 }
 
 rt_status rt_pool_trace(rt_pool* P, const RtJob* jobs, uint32_t num_jobs, uint32_t flags, void* stream) {
+  NvtxRange nvtx_range("rt_pool_trace");
   if (!P || (num_jobs && !jobs) || num_jobs > kMaxJobs || flags > RT_TRACE_ANY) {
     set_error("rt_pool_trace: bad argument (at most 8192 jobs; flags closest or any)");
     return RT_EINVAL;
@@ -667,6 +669,7 @@ rt_status rt_pool_trace(rt_pool* P, const RtJob* jobs, uint32_t num_jobs, uint32
 
 rt_status rt_pool_autotune(rt_pool* P, const RtJob* jobs, uint32_t num_jobs, uint32_t flags, void* stream,
                            uint32_t repeats) {
+  NvtxRange nvtx_range("rt_pool_autotune");
   if (!P || (num_jobs && !jobs) || num_jobs > kMaxJobs || flags > RT_TRACE_ANY) {
     set_error("rt_pool_autotune: bad argument");
     return RT_EINVAL;

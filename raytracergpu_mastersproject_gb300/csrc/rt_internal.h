@@ -38,7 +38,19 @@
 
 #include "../../include/rt_gb300.h"
 
+#include <nvtx3/nvToolsExt.h>
+
 namespace rtgb {
+
+// An NVTX range over a library entry point (shown by Nsight Systems and
+// usable as an ncu --nvtx filter); costs a function-pointer test when no tool
+// is attached.
+struct NvtxRange {
+  explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+  ~NvtxRange() { nvtxRangePop(); }
+  NvtxRange(const NvtxRange&) = delete;
+  NvtxRange& operator=(const NvtxRange&) = delete;
+};
 
 constexpr uint32_t kLeafBit = 0x80000000u;
 constexpr uint32_t kSphereBit = 0x40000000u;

@@ -382,6 +382,7 @@ void set_error(const std::string& msg);
 
 extern "C" rt_status rt_trace_noalloc(rt_scene* scene, const RtRay* d_rays, uint32_t n, RtHit* d_hits,
                                       uint32_t flags, void* stream) {
+  rtgb::NvtxRange nvtx_range("rt_trace_noalloc");
   using namespace rtgb;
   if (!scene || (n && (!d_rays || !d_hits)) || flags > RT_TRACE_ANY) {
     set_error("rt_trace_noalloc: bad argument");
