@@ -194,7 +194,7 @@ void dispatch_loop(rt_server* S) {
     S->launched++;
     S->stats.batches++;
     lk.unlock();
-    NvtxRange nvtx_range("rt_server batch");
+    rtgb::NvtxRange nvtx_range("rt_server batch");
     cudaError_t e = cudaEventCreateWithFlags(&b->done, cudaEventDisableTiming);
     for (Request* r : b->reqs)
       if (r->n && e == cudaSuccess)
