@@ -353,13 +353,9 @@ rt_status capture(rt_pool* P, LaunchSlot& sl, uint32_t* counter, int variant, in
   sl.graph = nullptr;
   PoolVariant& v = g_pool_variants[variant];
   PoolKernel k = v.k[any][big];
-  int& bps = v.bps[any][big];
-  if (bps < 0) {
-    int b = 0;
-    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k, v.threads, 0);
-    if (e != cudaSuccess) return cuda_err(e, "rt_pool: occupancy");
-    bps = b < 1 ? 1 : b;
-  }
+  int bps = 0;
+  if (cudaError_t oe = cached_blocks_per_sm(&v.bps[any][big], k, v.threads, &bps); oe != cudaSuccess)
+    return cuda_err(oe, "rt_pool: occupancy");
   cudaStream_t cs;
   cudaError_t e = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking);
   if (e != cudaSuccess) return cuda_err(e, "rt_pool: capture stream");

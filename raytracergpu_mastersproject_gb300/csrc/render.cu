@@ -616,13 +616,11 @@ template <int W, int STACK, bool STATS>
 cudaError_t launch_render_variant(const DeviceScene& S, const Cam& cam, uint32_t depth, uint32_t rs, float* accum,
                                   uint32_t w, uint32_t h, uint32_t spp, uint32_t shade, const float bg[3],
                                   uint32_t* counter, unsigned long long* stats, cudaStream_t st) {
-  static int blocks_per_sm = -1;
-  if (blocks_per_sm < 0) {
-    cudaError_t e =
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, k_render<W, STACK, STATS>, kThreads, 0);
-    if (e != cudaSuccess) return e;
-    if (blocks_per_sm < 1) blocks_per_sm = 1;
-  }
+  static int cache = -1;
+  int blocks_per_sm = 0;
+  if (cudaError_t e = cached_blocks_per_sm(&cache, k_render<W, STACK, STATS>, kThreads, &blocks_per_sm);
+      e != cudaSuccess)
+    return e;
   const uint32_t total = w * h;
   uint32_t blocks = (uint32_t)(device_sm_count() * blocks_per_sm);
   const uint32_t needed = (total + kThreads - 1) / kThreads;
@@ -638,13 +636,11 @@ template <int STACK, int T, int M, bool STATS>
 cudaError_t launch_render_step(const DeviceScene& S, const Cam& cam, uint32_t depth, uint32_t rs, float* accum,
                                uint32_t w, uint32_t h, uint32_t spp, uint32_t shade, const float bg[3],
                                uint32_t* counter, int refill, unsigned long long* stats, cudaStream_t st) {
-  static int blocks_per_sm = -1;
-  if (blocks_per_sm < 0) {
-    cudaError_t e =
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, k_render_step<STACK, T, M, STATS>, T, 0);
-    if (e != cudaSuccess) return e;
-    if (blocks_per_sm < 1) blocks_per_sm = 1;
-  }
+  static int cache = -1;
+  int blocks_per_sm = 0;
+  if (cudaError_t e = cached_blocks_per_sm(&cache, k_render_step<STACK, T, M, STATS>, T, &blocks_per_sm);
+      e != cudaSuccess)
+    return e;
   const uint32_t total = w * h;
   uint32_t blocks = (uint32_t)(device_sm_count() * blocks_per_sm);
   const uint32_t needed = (total + T - 1) / T;

@@ -42,6 +42,23 @@
 
 namespace rtgb {
 
+// Resident blocks per SM of `kernel` at `threads` per block, computed once per
+// cache slot.  Host threads may race to fill a slot; they compute the same
+// value, and the slot is read and written atomically.
+template <class K>
+cudaError_t cached_blocks_per_sm(int* slot, K kernel, int threads, int* out) {
+  int v = __atomic_load_n(slot, __ATOMIC_RELAXED);
+  if (v < 1) {
+    int b = 0;
+    const cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, kernel, threads, 0);
+    if (e != cudaSuccess) return e;
+    v = b < 1 ? 1 : b;
+    __atomic_store_n(slot, v, __ATOMIC_RELAXED);
+  }
+  *out = v;
+  return cudaSuccess;
+}
+
 // An NVTX range over a library entry point (shown by Nsight Systems and
 // usable as an ncu --nvtx filter); costs a function-pointer test when no tool
 // is attached.

@@ -307,13 +307,10 @@ cudaError_t launch_trace_tuned(const DeviceScene& S, const RtRay* rays, uint32_t
   const int big = S.stack_need > 64u ? 1 : 0;
   const int st = stats ? 1 : 0;
   TraceKernel k = v.k[st][wide][any][big];
-  int& bps = v.blocks_per_sm[st][wide][any][big];
-  if (bps < 0) {
-    int b = 0;
-    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k, v.threads, 0);
-    if (e != cudaSuccess) return e;
-    bps = b < 1 ? 1 : b;
-  }
+  int bps = 0;
+  if (cudaError_t e = cached_blocks_per_sm(&v.blocks_per_sm[st][wide][any][big], k, v.threads, &bps);
+      e != cudaSuccess)
+    return e;
   const uint32_t warps_per_block = (uint32_t)v.threads / 32u;
   const uint32_t warps_needed = (n + 31u) / 32u;
   uint64_t blocks = (uint64_t)device_sm_count() * (uint64_t)bps * (uint64_t)std::max(1, tune.grid_scale) / 100u;
@@ -326,11 +323,13 @@ cudaError_t launch_trace_tuned(const DeviceScene& S, const RtRay* rays, uint32_t
 }
 
 int device_sm_count() {
-  static int sms = -1;
-  if (sms < 0) {
+  static int cached = -1;
+  int sms = __atomic_load_n(&cached, __ATOMIC_RELAXED);
+  if (sms < 1) {
     int dev = 0;
     cudaGetDevice(&dev);
     if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms < 1) sms = 1;
+    __atomic_store_n(&cached, sms, __ATOMIC_RELAXED);
   }
   return sms;
 }
@@ -350,13 +349,9 @@ cudaError_t launch_trace_raw(const DeviceScene& S, const float4* rays, uint32_t 
                                   : k_trace_step<false, 192, T, M, false, true, R>)
                          : (stats ? k_trace_step<false, 64, T, M, true, true, R>
                                   : k_trace_step<false, 64, T, M, false, true, R>);
-  if (bps[k] < 0) {
-    int b = 0;
-    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, kern, T, 0);
-    if (e != cudaSuccess) return e;
-    bps[k] = b < 1 ? 1 : b;
-  }
-  uint64_t blocks = (uint64_t)device_sm_count() * (uint64_t)bps[k];
+  int per_sm = 0;
+  if (cudaError_t e = cached_blocks_per_sm(&bps[k], kern, T, &per_sm); e != cudaSuccess) return e;
+  uint64_t blocks = (uint64_t)device_sm_count() * (uint64_t)per_sm;
   if (n != 0xFFFFFFFFu) blocks = std::min<uint64_t>(blocks, ((uint64_t)n + T - 1) / T);
   if (blocks == 0) blocks = 1;
   kern<<<(uint32_t)blocks, T, 0, st>>>(S, rays, n, hits, counter, default_tuning().refill, stats, nullptr);
