@@ -308,3 +308,22 @@ def test_stream_release_frees_and_recreates_workspace(rt, cuda):
         rt.release_stream(st)  # nothing left to free
     assert np.array_equal(a, b)
     assert free1 >= free0
+
+
+@pytest.mark.parametrize("depth", [64, 70])
+def test_deep_paths_wavefront_and_step_kernel(rt, cuda, depth):
+    """Depth up to 64 runs the wavefront renderer, deeper frames the per-lane
+    step kernel; both equal the binary per-pixel kernel bit for bit.  Glass
+    spheres keep paths bouncing to the depth limit."""
+    tris, mats = rt.gen_spheres_scene(9, 8, 3, 0.05)
+    mats["materialType"] = rt.MAT_DIELECTRIC
+    mats["ior"] = 1.5
+    mats["albedo"][:, :3] = 1.0
+    ubo = rt.make_ubo((0.0, 3.0, 28.0), (0.0, 0.0, 0.0), fov=40.0, depth=depth, random_state=4,
+                      num_triangles=len(tris), num_materials=len(mats))
+    kw = {"shade_mode": rt.SHADE_EXTENDED, "background": (0.6, 0.7, 1.0)}
+    with rt.Scene(tris, materials=mats, node_width=2) as s2, rt.Scene(tris, materials=mats, node_width=4) as s4:
+        a = gpu_render(rt, cuda, s2, ubo, 48, 27, 2, **kw)
+        b = gpu_render(rt, cuda, s4, ubo, 48, 27, 2, **kw)
+    assert np.array_equal(a, b)
+    assert a[0::4].max() > 0.1
