@@ -33,7 +33,7 @@ __device__ __forceinline__ bool tri_test(const void* tris, uint32_t slot, float 
   const float denom = r0.x * dx + r0.y * dy + r0.z * dz;
   if (fabsf(denom) < 0.0001f) return false;
   const float t = (r0.w - (r0.x * ox + r0.y * oy + r0.z * oz)) / denom;
-  if (!(t >= tmin && t <= tmax)) return false;
+  if (!(t >= tmin && t <= tmax)) return false;  // a NaN t misses
   const float4 r1 = ldg4(tris, 4u * slot + 1u);  // w.xyz, v0.x
   const float4 r2 = ldg4(tris, 4u * slot + 2u);  // v0.y, v0.z, u.x, u.y
   const float4 r3 = ldg4(tris, 4u * slot + 3u);  // u.z, v.x, v.y, v.z
@@ -120,7 +120,10 @@ __device__ __forceinline__ void trav_set_close(Trav& s, float t) {
 
 // Loads one ray into the state; the caller prepares its stack.
 __device__ __forceinline__ void trav_init_ray(Trav& s, const float4 o_tmin, const float4 d_tmax, uint32_t root) {
-  s.ox = o_tmin.x; s.oy = o_tmin.y; s.oz = o_tmin.z; s.tmin = o_tmin.w;
+  // A NaN bound rejects nothing in the reference's t < tMin || tMax < t, as
+  // -inf / +inf do, which keeps the tests below NaN-free.
+  const float inf = __int_as_float(0x7f800000);
+  s.ox = o_tmin.x; s.oy = o_tmin.y; s.oz = o_tmin.z; s.tmin = o_tmin.w == o_tmin.w ? o_tmin.w : -inf;
   s.dx = d_tmax.x; s.dy = d_tmax.y; s.dz = d_tmax.z;
   // Zero (or smaller) direction components become +-2^-64, so 1/d stays
   // within 2^64: with 4-wide steps up to 2^kMaxWideExp the node scale
@@ -130,13 +133,21 @@ __device__ __forceinline__ void trav_init_ray(Trav& s, const float4 o_tmin, cons
   s.iy = 1.0f / (fabsf(s.dy) > eps ? s.dy : copysignf(eps, s.dy));
   s.iz = 1.0f / (fabsf(s.dz) > eps ? s.dz : copysignf(eps, s.dz));
   s.cull_lo = fmaf(-fabsf(s.tmin), kCullRel, s.tmin);
-  trav_set_close(s, d_tmax.w);
+  trav_set_close(s, d_tmax.w == d_tmax.w ? d_tmax.w : inf);
   s.best = kNoBest;
   s.node = root;
   s.leaf = 0u;
   if (root > kSentinel) {  // the whole tree is one leaf
     s.leaf = root;
     s.node = kSentinel;
+  }
+  // A non-finite origin or direction component fails the reference's root
+  // box test (its slab parameters are infinite or NaN), so the ray misses.
+  const float big = 3.40282347e+38f;
+  if (!(fabsf(s.ox) <= big && fabsf(s.oy) <= big && fabsf(s.oz) <= big && fabsf(s.dx) <= big &&
+        fabsf(s.dy) <= big && fabsf(s.dz) <= big)) {
+    s.node = kSentinel;
+    s.leaf = 0u;
   }
   s.sp = 0;
   s.nvis = 0;

@@ -423,3 +423,41 @@ def test_hit_t_against_fp64(rt, orc, cuda):
     i3, t3, err3 = _t64_errors(orc, tris3, rays3, got3)
     assert len(i3) > 10_000
     assert np.all(err3 <= 1e-5 * np.maximum(np.abs(t3), 1.0))
+
+
+def test_degenerate_rays(rt, orc, cuda):
+    """NaN and infinite components, an all-zero direction, tmin > tmax, an
+    empty interval and negative tmin: no fault, and the same answer as the
+    oracle's restatement.  A NaN origin or direction gives NaN parameters,
+    which never hit; a NaN tmax rejects nothing, as in the reference's
+    `t < tMin || tMax < t`, so it acts as +inf."""
+    tris = rt.gen_soup(41, 0, 20_000, 1.0, 0.01)
+    base = rt.gen_rays(41, 0, 4_096, 1.0, 1e-4, float("inf"))
+    rays = np.concatenate([base] * 8)
+    k = len(base)
+    nan, inf = np.float32(np.nan), np.float32(np.inf)
+    rays["org"][0 * k:1 * k, 0] = nan
+    rays["dir"][1 * k:2 * k, 1] = nan
+    rays["dir"][2 * k:3 * k] = 0.0
+    rays["tmin"][3 * k:4 * k] = 2.0
+    rays["tmax"][3 * k:4 * k] = 1.0
+    rays["tmin"][4 * k:5 * k] = 0.25
+    rays["tmax"][4 * k:5 * k] = 0.25
+    rays["tmin"][5 * k:6 * k] = -1.0
+    rays["org"][6 * k:7 * k, 2] = inf
+    rays["tmax"][7 * k:8 * k] = nan
+    with rt.Scene(tris, node_width=4) as s4, rt.Scene(tris, node_width=2) as s2:
+        got4 = dev_trace(rt, cuda, s4, rays)
+        got4s = dev_trace(rt, cuda, s4, rays, sort=True)
+        got2 = dev_trace(rt, cuda, s2, rays)
+        any4 = dev_trace(rt, cuda, s4, rays, any_hit=True)
+        ref, _ = orc.trace(orc.Scene(tris, s4.nodes()), rays, canonical=True)
+    for got in (got4, got2):
+        assert_parity(orc, tris, rays, ref, got)
+    assert np.array_equal(got4.view(np.uint64), got4s.view(np.uint64))
+    assert np.array_equal(any4["prim"] != orc.NO_HIT, ref["prim"] != orc.NO_HIT)
+    for blk in (0, 1, 2, 3):  # NaN origin/direction, zero direction, tmin > tmax
+        assert np.all(got4["prim"][blk * k:(blk + 1) * k] == orc.NO_HIT), blk
+    # NaN tmax behaves as +inf: the same hits as the unmodified rays
+    base_hits = dev_trace(rt, cuda, rt.Scene(tris, node_width=4), base)
+    assert np.array_equal(got4[7 * k:].view(np.uint64), base_hits.view(np.uint64))
