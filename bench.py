@@ -47,7 +47,7 @@ CPU_SAMPLE = 2_097_152
 # DRAM bytes per ray of k_trace_step on the full config-3 BVH, from the ncu
 # capture summarised in profiles/k_trace_step_config3.md (2,097,152 rays,
 # dram__bytes_read.sum + dram__bytes_write.sum = 2.502 GB).
-DRAM_BYTES_PER_RAY = (1.400946e9 + 60.410112e6) / 2_097_152  # ncu, 2 Mi-ray launch on the config-3 tree
+DRAM_BYTES_PER_RAY = (1.397093e9 + 60.756992e6) / 2_097_152  # ncu, 2 Mi-ray launch on the config-3 tree
 
 
 def parse():
