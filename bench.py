@@ -44,9 +44,8 @@ N_TRIS = 4_194_304
 N_RAYS = 16_777_216
 SEED = 3
 CPU_SAMPLE = 2_097_152
-# DRAM bytes per ray of k_trace_step on the full config-3 BVH, from the ncu
-# capture summarised in profiles/k_trace_step_config3.md (2,097,152 rays,
-# dram__bytes_read.sum + dram__bytes_write.sum = 2.502 GB).
+# DRAM bytes per ray of k_trace_step on the full config-3 BVH: one ncu capture
+# of a 2,097,152-ray launch, dram__bytes_read.sum + dram__bytes_write.sum.
 DRAM_BYTES_PER_RAY = (1.397093e9 + 60.756992e6) / 2_097_152  # ncu, 2 Mi-ray launch on the config-3 tree
 
 
@@ -185,15 +184,25 @@ def workload(n_tris: int, n_rays: int):
 
 def cpu_leg(tris, nodes, rays, sample: int, trav_nodes=None) -> tuple[dict, dict]:
     """CPU baseline: the oracle's reference-order traversal of the S1 tree
-    (`nodes`, the reference's own) on `sample` rays with every host thread;
-    plus canonical traversal counts (work per ray) on the tree the kernel
-    traverses (`trav_nodes`, default the S1 tree)."""
+    (`nodes`, the reference's own) with every host thread, the median of 5
+    timed runs on a quarter of `sample` rays, plus one run over all `sample`
+    rays whose hits check the GPU's; single-thread rates on small samples;
+    canonical traversal counts (work per ray) on the tree the kernel traverses
+    (`trav_nodes`, default the S1 tree)."""
     from oracle import oracle as orc
 
     orc.build()
     S = orc.Scene(tris, nodes)
     cores = os.cpu_count() or 1
     sub = np.ascontiguousarray(rays[:sample])
+
+    def rate(scene, r, canonical, threads):
+        t0 = time.perf_counter()
+        orc.trace(scene, r, canonical=canonical, nthreads=threads)
+        return len(r) / (time.perf_counter() - t0) / 1e9
+
+    quarter = np.ascontiguousarray(rays[:max(1, sample // 4)])
+    runs = [rate(S, quarter, False, cores) for _ in range(5)]
     t0 = time.perf_counter()
     ref_hits, st = orc.trace(S, sub, canonical=False, nthreads=cores)
     dt = time.perf_counter() - t0
@@ -202,11 +211,18 @@ def cpu_leg(tris, nodes, rays, sample: int, trav_nodes=None) -> tuple[dict, dict
     t1 = time.perf_counter()
     can_hits, cst = orc.trace(St, cnt, canonical=True, nthreads=cores)
     dt_can = time.perf_counter() - t1
+    one_ref = np.ascontiguousarray(rays[:max(1, sample // 32)])
+    one_can = np.ascontiguousarray(rays[:max(1, sample // 16)])
+    single = {"reference_order": rate(S, one_ref, False, 1), "reference_order_rays": len(one_ref),
+              "canonical": rate(St, one_can, True, 1), "canonical_rays": len(one_can), "unit": UNIT}
     counts = {"node_boxes_per_ray": float(cst[0]) / len(cnt), "tri_tests_per_ray": float(cst[1]) / len(cnt),
               "sample": len(cnt)}
-    base = {"value": len(sub) / dt / 1e9, "unit": UNIT, "cores": cores, "kind": "port",
-            "sample": f"first {len(sub)} rays of the config-3 batch, oracle restatement of hitBVH "
-                      f"(reference order, no culling, sorted-leaf BVH), {cores} threads, {dt:.2f} s",
+    base = {"value": float(np.median(runs)), "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": f"median of 5 runs over the first {len(quarter)} rays of the config-3 batch, oracle "
+                      f"restatement of hitBVH (reference order, no culling, sorted-leaf BVH), {cores} threads",
+            "runs": runs,
+            "full_sample": {"rays": len(sub), "value": len(sub) / dt / 1e9, "seconds": dt},
+            "single_thread": single,
             "canonical": {"value": len(cnt) / dt_can / 1e9, "unit": UNIT, "cores": cores,
                           "sample": f"first {len(cnt)} rays, the same restatement with near-child-first "
                                     f"order and interval culling (the kernels' order; same hits) over "
@@ -551,8 +567,8 @@ def run_ours(args):
         full3 = (args.tris, n) == (N_TRIS, N_RAYS) and sort and info.node_width == 4
         roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                 "traffic": DRAM_BYTES_PER_RAY * n if full3 else None,
-                "traffic_note": "ncu dram bytes of a 2,097,152-ray launch on the same BVH, scaled by rays "
-                                "(profiles/k_trace_step_config3.md)" if full3 else "not captured for this shape",
+                "traffic_note": "ncu dram bytes of a 2,097,152-ray launch on the same BVH, scaled by rays"
+                                if full3 else "not captured for this shape",
                 "peak_kind": peak_kind,
                 "bytes_per_ray": b_ray, "node_boxes_per_ray": counts["node_boxes_per_ray"],
                 "tri_tests_per_ray": counts["tri_tests_per_ray"],

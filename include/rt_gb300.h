@@ -49,7 +49,7 @@ typedef enum rt_status {
   RT_EBUSY = 6,       /* admission refused for now (serving)                  */
   RT_ECANCELED = 7,   /* request cancelled                                    */
   RT_ENOTFOUND = 8,   /* unknown scene / request id                           */
-  RT_EUNSUPPORTED = 9 /* option not supported by this build                   */
+  RT_EUNSUPPORTED = 9 /* option not supported by this library                 */
 } rt_status;
 
 /* ------------------------------------------------ enums of the reference */

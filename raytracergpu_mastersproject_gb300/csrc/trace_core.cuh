@@ -350,8 +350,7 @@ struct RingStack {
   }
 };
 
-// Byte i of w as a float: the byte is placed under exponent 2^23 (0x4B000000)
-// and 2^23 subtracted, both exact.
+// 3-input max / min (a PTX form of sm_100 and later).
 __device__ __forceinline__ float fmax3(float a, float b, float c) {
   float d;
   asm("max.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
