@@ -557,7 +557,12 @@ rt_status rt_trace_host(rt_scene* scene, const RtRay* h_rays, uint32_t n, RtHit*
     else
       cudaGetLastError();  // an unregistered pointer is not an error here
   }
-  const uint32_t growth = direct ? 8u : 4u;
+  static const uint32_t kGrowth = [] {
+    const char* e = std::getenv("RT_HOST_CHUNK_GROWTH");
+    const long v = e ? std::atol(e) : 0;
+    return v >= 2 && v <= 64 ? (uint32_t)v : 0u;
+  }();
+  const uint32_t growth = kGrowth ? kGrowth : (direct ? 8u : 4u);
   const uint32_t chunk = std::min<uint32_t>(n, direct ? (1u << 24) : (1u << 23));  // buffer capacity
   const size_t ray_bytes = (size_t)chunk * sizeof(RtRay), hit_bytes = direct ? 0 : (size_t)chunk * sizeof(RtHit);
   const size_t per = ray_bytes + hit_bytes;
