@@ -122,6 +122,19 @@ static rt_status ensure_sort_scratch(Workspace* w, size_t need) {
   return RT_OK;
 }
 
+// The helper streams and events of rt_trace_host and the wavefront renderer,
+// created on first use.
+static rt_status ensure_helpers(Workspace* w) {
+  if (w->copy_in) return RT_OK;
+  cudaError_t e;
+  if ((e = cudaStreamCreateWithFlags(&w->copy_in, cudaStreamNonBlocking)) != cudaSuccess) return cuda_fail(e, "stream");
+  if ((e = cudaStreamCreateWithFlags(&w->copy_out, cudaStreamNonBlocking)) != cudaSuccess) return cuda_fail(e, "stream");
+  if ((e = cudaStreamCreateWithFlags(&w->trace2, cudaStreamNonBlocking)) != cudaSuccess) return cuda_fail(e, "stream");
+  for (auto& ev : w->ev)
+    if ((e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming)) != cudaSuccess) return cuda_fail(e, "event");
+  return RT_OK;
+}
+
 static size_t sort_slot_bytes(uint32_t n) { return (reorder_scratch_bytes(n) + 255) & ~(size_t)255; }
 
 // Reorders the batch when RT_TRACE_SORT is set; *order = nullptr otherwise.
@@ -581,13 +594,7 @@ rt_status rt_trace_host(rt_scene* scene, const RtRay* h_rays, uint32_t n, RtHit*
   }
   const size_t slot = sort_slot_bytes(chunk);
   if ((flags & RT_TRACE_SORT) && (s = ensure_sort_scratch(w, 2 * slot)) != RT_OK) return s;
-  if (!w->copy_in) {
-    if ((e = cudaStreamCreateWithFlags(&w->copy_in, cudaStreamNonBlocking)) != cudaSuccess) return cuda_fail(e, "stream");
-    if ((e = cudaStreamCreateWithFlags(&w->copy_out, cudaStreamNonBlocking)) != cudaSuccess) return cuda_fail(e, "stream");
-    if ((e = cudaStreamCreateWithFlags(&w->trace2, cudaStreamNonBlocking)) != cudaSuccess) return cuda_fail(e, "stream");
-    for (auto& ev : w->ev)
-      if ((e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming)) != cudaSuccess) return cuda_fail(e, "event");
-  }
+  if ((s = ensure_helpers(w)) != RT_OK) return s;
   char* base = static_cast<char*>(w->stage);
   RtRay* drays[2] = {reinterpret_cast<RtRay*>(base), reinterpret_cast<RtRay*>(base + per)};
   RtHit* dhits[2] = {reinterpret_cast<RtHit*>(base + ray_bytes), reinterpret_cast<RtHit*>(base + per + ray_bytes)};
@@ -701,8 +708,23 @@ static rt_status render_impl(rt_scene* scene, const RtRaytraceUBO* ubo, float* d
   unsigned long long* stats = h_counts ? reinterpret_cast<unsigned long long*>(w->counters + 8) : nullptr;
   const uint32_t mode = (o.shade_mode == RT_SHADE_EXTENDED ? kRenderExtended : 0u) |
                         ((o.flags & RT_RENDER_TRACE_EVERY_PRIMARY) ? kRenderTraceEveryPrimary : 0u);
+  RenderStreams rs;
+  if (wave_paths) {
+    if ((s = ensure_helpers(w)) != RT_OK) return s;
+    static const int kLanes = [] {
+      const char* v = std::getenv("RT_RENDER_LANES");
+      const int x = v ? std::atoi(v) : 0;
+      return x >= 1 && x <= kWaveLanes ? x : 2;
+    }();
+    rs.extra = kLanes - 1;
+    rs.streams[0] = w->trace2;
+    rs.streams[1] = w->copy_out;
+    rs.fork = w->ev[6];
+    rs.join[0] = w->ev[7];
+    rs.join[1] = w->ev[5];
+  }
   e = launch_render(scene->d, cam, ubo->maxRayTraceDepth, ubo->randomState, d_accum, width, height, spp, mode,
-                    o.background, w->counters, stream, stats, w->wave, wave_paths);
+                    o.background, w->counters, stream, stats, w->wave, wave_paths, &rs);
   if (e != cudaSuccess) return cuda_fail(e, "rt_render: launch");
   if (h_counts) {
     unsigned long long hc[3] = {0, 0, 0};

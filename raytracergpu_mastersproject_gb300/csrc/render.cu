@@ -555,41 +555,83 @@ WaveBufs wave_bufs(void* scratch, uint64_t paths, uint32_t depth) {
   return w;
 }
 
+// Scratch of one stream's part for `paths` paths.
+size_t wave_part_bytes(uint64_t paths, uint32_t depth) {
+  const size_t b = (size_t)paths * kWaveBytesPerPath + 8 * 256 + 16 * ((size_t)depth + 1);
+  return (b + 255) & ~(size_t)255;  // the next stream's part starts 256-byte aligned
+}
+
+// A frame below this many paths per chunk stays one chunk on one stream.
+constexpr uint64_t kWaveMinChunkPaths = 1u << 16;
+
+// Pixel chunks rotate over the caller's stream and the extra streams given,
+// each stream with its own part of the scratch: chunk c+1's bounce levels run
+// while chunk c's are in flight, so one chunk's launch tails (the drain of a
+// persistent trace grid, a short shading pass) overlap another's work.  All
+// samples of a pixel stay in one chunk, in order, so the accumulator and its
+// RNG carry are the same as with one stream.
 template <bool STATS>
 cudaError_t launch_render_wave(const DeviceScene& S, const Cam& cam, uint32_t depth, uint32_t rs, float* accum_f,
                                uint32_t Wd, uint32_t H, uint32_t spp, uint32_t mode, const float bg[3],
                                uint32_t* counter, unsigned long long* stats, void* scratch, uint64_t max_paths,
-                               cudaStream_t st) {
+                               cudaStream_t st, const RenderStreams* streams) {
   float4* accum = reinterpret_cast<float4*>(accum_f);
   const uint32_t total = Wd * H;
   const uint32_t per_path = (mode & kRenderTraceEveryPrimary) ? 1u : 0u;
-  const uint32_t ns_pass = (uint32_t)std::min<uint64_t>(spp, max_paths);
-  const uint32_t q_chunk = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(total, max_paths / ns_pass));
-  const WaveBufs B = wave_bufs(scratch, max_paths, depth);
+  // Streams used: all given, unless the whole frame fits the scratch and
+  // splitting it would leave chunks below kWaveMinChunkPaths.
+  const uint64_t frame_paths = (uint64_t)total * spp;
+  int used = 1 + (streams ? std::min(streams->extra, kWaveLanes - 1) : 0);
+  while (used > 1 && frame_paths <= max_paths && frame_paths < (uint64_t)used * kWaveMinChunkPaths) --used;
+  const uint64_t cap = (max_paths + used - 1) / used;  // paths per stream's scratch part
+  const uint32_t ns_pass = (uint32_t)std::min<uint64_t>(spp, cap);
+  const uint32_t q_cap = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(total, cap / ns_pass));
+  // equal chunks, as many as the capacity needs, a multiple of the streams
+  uint64_t n_chunks = std::max<uint64_t>(((uint64_t)total + q_cap - 1) / q_cap, (uint64_t)used);
+  n_chunks = (n_chunks + used - 1) / used * used;
+  const uint32_t q_chunk = (uint32_t)(((uint64_t)total + n_chunks - 1) / n_chunks);
+  WaveBufs Bs[kWaveLanes];
+  cudaStream_t sts[kWaveLanes];
+  for (int k = 0; k < used; ++k) {
+    Bs[k] = wave_bufs(static_cast<char*>(scratch) + (size_t)k * wave_part_bytes(cap, depth), cap, depth);
+    sts[k] = k == 0 ? st : streams->streams[k - 1];
+  }
   const uint32_t sms = (uint32_t)device_sm_count();
   unsigned long long* trace_stats = STATS ? stats + 1 : nullptr;
   cudaError_t e;
-  for (uint32_t pix0 = 0; pix0 < total; pix0 += q_chunk) {
+  if (used > 1) {
+    if ((e = cudaEventRecord(streams->fork, st)) != cudaSuccess) return e;
+    for (int k = 1; k < used; ++k)
+      if ((e = cudaStreamWaitEvent(sts[k], streams->fork, 0)) != cudaSuccess) return e;
+  }
+  uint32_t chunk = 0;
+  for (uint32_t pix0 = 0; pix0 < total; pix0 += q_chunk, ++chunk) {
     const uint32_t q = std::min(q_chunk, total - pix0);
+    const WaveBufs& B = Bs[chunk % (uint32_t)used];
+    const cudaStream_t cs = sts[chunk % (uint32_t)used];
     for (uint32_t s0 = 0; s0 < spp; s0 += ns_pass) {
       const uint32_t ns = std::min(ns_pass, spp - s0);
       const uint32_t np = q * ns;
-      if ((e = cudaMemsetAsync(B.cnt, 0, 16 * ((size_t)depth + 1), st)) != cudaSuccess) return e;
+      if ((e = cudaMemsetAsync(B.cnt, 0, 16 * ((size_t)depth + 1), cs)) != cudaSuccess) return e;
       const uint32_t gb = std::min<uint32_t>(sms * 8, (q + 255) / 256);
-      k_wave_seed<<<gb, 256, 0, st>>>(cam, rs, accum, Wd, pix0, q, ns, per_path, B.rng0, B.rays[0]);
+      k_wave_seed<<<gb, 256, 0, cs>>>(cam, rs, accum, Wd, pix0, q, ns, per_path, B.rng0, B.rays[0]);
       for (uint32_t l = 0; l < depth; ++l) {
         const float4* r = B.rays[l & 1u];
         if ((e = launch_trace_raw(S, r, l == 0 ? (per_path ? np : q) : 0xFFFFFFFFu, B.hits, B.cnt + 4u * l,
-                                  trace_stats, st)) != cudaSuccess)
+                                  trace_stats, cs)) != cudaSuccess)
           return e;
         const uint32_t gs = l == 0 ? std::min<uint32_t>(sms * 8, (np + 255) / 256) : sms * 8;
-        k_wave_shade<STATS><<<gs, 256, 0, st>>>(S, l, depth, np, q, ns, per_path, mode, bg[0], bg[1], bg[2], B.state,
+        k_wave_shade<STATS><<<gs, 256, 0, cs>>>(S, l, depth, np, q, ns, per_path, mode, bg[0], bg[1], bg[2], B.state,
                                                 B.rng0, r, B.list[l & 1u], B.hits, B.rays[(l + 1u) & 1u],
                                                 B.list[(l + 1u) & 1u], B.cnt, counter + 1, stats);
       }
-      k_wave_accum<<<gb, 256, 0, st>>>(accum, pix0, q, ns, B.state);
+      k_wave_accum<<<gb, 256, 0, cs>>>(accum, pix0, q, ns, B.state);
       if ((e = cudaGetLastError()) != cudaSuccess) return e;
     }
+  }
+  for (int k = 1; k < used; ++k) {
+    if ((e = cudaEventRecord(streams->join[k - 1], sts[k])) != cudaSuccess) return e;
+    if ((e = cudaStreamWaitEvent(st, streams->join[k - 1], 0)) != cudaSuccess) return e;
   }
   return cudaGetLastError();
 }
@@ -673,11 +715,11 @@ template <bool STATS>
 cudaError_t launch_render_impl(const DeviceScene& s, const Cam& c, uint32_t depth, uint32_t random_state, float* accum,
                                uint32_t w, uint32_t h, uint32_t spp, uint32_t mode, const float bg[3],
                                uint32_t* counter, unsigned long long* stats, void* scratch, uint64_t scratch_paths,
-                               cudaStream_t st) {
+                               cudaStream_t st, const RenderStreams* rs) {
   const RenderTuning& tn = render_tuning();
   if (s.width == 4 && depth > 0u && depth <= kWaveMaxDepth && tn.variant == 4 && scratch && scratch_paths > 0)
     return launch_render_wave<STATS>(s, c, depth, random_state, accum, w, h, spp, mode, bg, counter, stats, scratch,
-                                     scratch_paths, st);
+                                     scratch_paths, st, rs);
   if (s.width == 4 && depth > 0u && tn.variant >= 1 && tn.variant <= 4) {  // 4: depth beyond the wavefront's
     const bool big = s.stack_need > 64u;
 #define RT_STEP(STK, T, M)                                                                                         \
@@ -700,15 +742,15 @@ cudaError_t launch_render_impl(const DeviceScene& s, const Cam& c, uint32_t dept
 cudaError_t launch_render(const DeviceScene& s, const float cam[12], uint32_t depth, uint32_t random_state,
                           float* accum, uint32_t w, uint32_t h, uint32_t spp, uint32_t mode, const float bg[3],
                           uint32_t* counter, void* stream, unsigned long long* stats, void* scratch,
-                          uint64_t scratch_paths) {
+                          uint64_t scratch_paths, const RenderStreams* rs) {
   Cam c;
   for (int k = 0; k < 12; ++k) c.v[k] = cam[k];
   cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
   if (stats)
     return launch_render_impl<true>(s, c, depth, random_state, accum, w, h, spp, mode, bg, counter, stats, scratch,
-                                    scratch_paths, st);
+                                    scratch_paths, st, rs);
   return launch_render_impl<false>(s, c, depth, random_state, accum, w, h, spp, mode, bg, counter, nullptr, scratch,
-                                   scratch_paths, st);
+                                   scratch_paths, st, rs);
 }
 
 bool render_uses_scratch(const DeviceScene& s, uint32_t depth) {
@@ -716,7 +758,10 @@ bool render_uses_scratch(const DeviceScene& s, uint32_t depth) {
 }
 
 size_t render_scratch_bytes(uint64_t paths, uint32_t depth) {
-  return (size_t)paths * kWaveBytesPerPath + 8 * 256 + 16 * ((size_t)depth + 1);
+  size_t most = 0;  // any split of the paths over 1..kWaveLanes streams fits
+  for (uint64_t k = 1; k <= (uint64_t)kWaveLanes; ++k)
+    most = std::max(most, (size_t)k * wave_part_bytes((paths + k - 1) / k, depth));
+  return most;
 }
 
 cudaError_t launch_accum_clear(float* accum, uint32_t w, uint32_t h, void* stream) {

@@ -197,13 +197,25 @@ cudaError_t launch_trace_raw(const DeviceScene& s, const float4* rays, uint32_t 
 // launch_render mode bits
 constexpr uint32_t kRenderExtended = 1u;            // RT_SHADE_EXTENDED
 constexpr uint32_t kRenderTraceEveryPrimary = 2u;   // RT_RENDER_TRACE_EVERY_PRIMARY
+// Extra streams for the wavefront renderer (pixel chunks rotate over the
+// caller's stream and these), with an event to fork them from the caller's
+// stream and one per extra stream to join them back (none: one stream).
+struct RenderStreams {
+  int extra = 0;  // at most 3
+  cudaStream_t streams[3] = {nullptr, nullptr, nullptr};
+  cudaEvent_t fork = nullptr;
+  cudaEvent_t join[3] = {nullptr, nullptr, nullptr};
+};
 cudaError_t launch_render(const DeviceScene& s, const float cam[12], uint32_t depth, uint32_t random_state,
                           float* accum, uint32_t w, uint32_t h, uint32_t spp, uint32_t mode,
                           const float bg[3], uint32_t* counter, void* stream,
                           unsigned long long* stats = nullptr,  // stats: queries, nodes, primitives
-                          void* scratch = nullptr, uint64_t scratch_paths = 0);
+                          void* scratch = nullptr, uint64_t scratch_paths = 0, const RenderStreams* rs = nullptr);
 // The wavefront renderer (4-wide trees) needs scratch of render_scratch_bytes
-// for up to `paths` paths in flight; the frame is split into passes that fit.
+// for up to `paths` paths in flight, split in one part per stream (up to
+// kWaveLanes) so that pixel chunks run their bounce levels on several streams
+// at once; the frame is split into chunks that fit.
+constexpr int kWaveLanes = 3;
 bool render_uses_scratch(const DeviceScene& s, uint32_t depth);
 size_t render_scratch_bytes(uint64_t paths, uint32_t depth);
 cudaError_t launch_accum_clear(float* accum, uint32_t w, uint32_t h, void* stream);

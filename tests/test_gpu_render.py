@@ -221,10 +221,12 @@ def test_shared_first_hit_is_exact(rt, cuda):
 
 @pytest.mark.parametrize("paths", ["777", "4"])
 def test_wavefront_passes_match(rt, cuda, tmp_path, paths):
-    """The wavefront renderer splits a frame into passes when its paths do not
-    fit the scratch: room for 777 paths gives chunks of 86 pixels x 9 samples;
-    room for 4 gives one pixel at a time in sample passes of 4, 4 and 1 (the
-    alpha carry links the passes).  The frame is unchanged either way."""
+    """The wavefront renderer splits a frame into pixel chunks when its paths
+    do not fit the scratch, alternating two scratch halves and two streams:
+    room for 777 paths gives chunks of 43 pixels x 9 samples; room for 4 gives
+    one pixel at a time in sample passes of 2, 2, 2, 2 and 1 (the alpha carry
+    links the passes).  The frame is unchanged either way (the reference frame
+    here, 13,833 paths, runs as one chunk on one stream)."""
     import os
     import subprocess
     import sys
