@@ -260,6 +260,54 @@ np.save({repr(str(tmp_path / "b.npy"))}, acc.cpu().numpy())
     assert np.array_equal(np.load(tmp_path / "b.npy"), a)
 
 
+@pytest.mark.parametrize("lanes", ["1", "3"])
+def test_render_lanes_match(rt, cuda, tmp_path, lanes):
+    """A frame of 230,400 paths is split into pixel chunks over two streams by
+    default; one stream (RT_RENDER_LANES=1) or three give the same frame bit
+    for bit, and so do the work counters of rt_render_count."""
+    import os
+    import subprocess
+    import sys
+
+    w, h, spp = 320, 180, 4
+    tris, mats = lit_scene(rt)
+    ubo = rt.make_ubo((0.0, 0.5, 4.0), (0.0, 0.0, 0.0), fov=60.0, depth=6, random_state=5)
+    kw = {"shade_mode": rt.SHADE_EXTENDED, "background": (0.3, 0.4, 0.5)}
+    with rt.Scene(tris, materials=mats, node_width=4) as sc:
+        a = gpu_render(rt, cuda, sc, ubo, w, h, spp, **kw)
+        acc = cuda.empty(w * h * 4, dtype=cuda.float32, device="cuda")
+        rt.accum_clear(acc, w, h)
+        counts = sc.render_count(ubo, acc, w, h, spp, **kw)
+        cuda.cuda.synchronize()
+        assert np.array_equal(acc.cpu().numpy(), a)
+    code = f"""
+import numpy as np, torch, sys
+sys.path.insert(0, {repr(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))})
+import raytracergpu_mastersproject_gb300 as rt
+sph = rt.gen_icosphere(3, (0.0, 0.0, 0.0), 1.0, 0)
+tris = np.concatenate([sph, rt.gen_config1()[0][-2:]])
+mats = np.zeros(2, rt.MATERIAL_DTYPE)
+mats[0]["albedo"][:3] = (0.73, 0.33, 0.25); mats[0]["materialType"] = rt.MAT_DIFFUSE
+mats[1]["albedo"][:3] = (3.0, 3.0, 3.0); mats[1]["materialType"] = rt.MAT_LIGHT
+ubo = rt.make_ubo((0.0, 0.5, 4.0), (0.0, 0.0, 0.0), fov=60.0, depth=6, random_state=5)
+kw = dict(shade_mode=rt.SHADE_EXTENDED, background=(0.3, 0.4, 0.5))
+acc = torch.empty({w} * {h} * 4, dtype=torch.float32, device="cuda")
+with rt.Scene(tris, materials=mats, node_width=4) as sc:
+    rt.accum_clear(acc, {w}, {h})
+    sc.render(ubo, acc, {w}, {h}, {spp}, **kw)
+    torch.cuda.synchronize()
+    np.save({repr(str(tmp_path / "b.npy"))}, acc.cpu().numpy())
+    rt.accum_clear(acc, {w}, {h})
+    c = sc.render_count(ubo, acc, {w}, {h}, {spp}, **kw)
+    np.save({repr(str(tmp_path / "c.npy"))}, np.array(c, dtype=np.uint64))
+"""
+    env = dict(os.environ, RT_RENDER_LANES=lanes)
+    p = subprocess.run([sys.executable, "-c", code], env=env, capture_output=True, text=True, timeout=300)
+    assert p.returncode == 0, p.stderr
+    assert np.array_equal(np.load(tmp_path / "b.npy"), a)
+    assert tuple(int(x) for x in np.load(tmp_path / "c.npy")) == tuple(counts)
+
+
 def test_deep_stack_render_matches_per_pixel(rt, cuda):
     """A dense cluster of large triangles keeps traversal stacks far past the
     shared-memory ring; the wavefront frame equals the binary per-pixel one."""
