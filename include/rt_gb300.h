@@ -434,7 +434,11 @@ typedef struct RtRenderOptions {
 /* The S2 pass (RaytracerBVH.cpp:998-1078): spp samples per pixel of
  * raytraceBVH.comp:main, each adding its colour to d_accum (W*H float4,
  * row-major, pixel (x,y) at index y*W+x) and leaving the RNG carry in alpha,
- * exactly as spp back-to-back dispatches would.  opt may be NULL (reference). */
+ * exactly as spp back-to-back dispatches would.  opt may be NULL (reference).
+ * Stream-ordered on `stream`: the library may fork part of the frame onto a
+ * helper stream of its own, which waits for `stream` first and which
+ * `stream` waits for before anything enqueued after this call (an event
+ * fork/join, so the call can also be captured into a CUDA graph). */
 rt_status rt_render(rt_scene* scene, const RtRaytraceUBO* ubo, float* d_accum,
                     uint32_t width, uint32_t height, uint32_t spp,
                     const RtRenderOptions* opt, void* stream);
