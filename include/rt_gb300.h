@@ -438,7 +438,7 @@ typedef struct RtRenderOptions {
  * Stream-ordered on `stream`: the library may fork part of the frame onto a
  * helper stream of its own, which waits for `stream` first and which
  * `stream` waits for before anything enqueued after this call (an event
- * fork/join, so the call can also be captured into a CUDA graph). */
+ * fork/join). */
 rt_status rt_render(rt_scene* scene, const RtRaytraceUBO* ubo, float* d_accum,
                     uint32_t width, uint32_t height, uint32_t spp,
                     const RtRenderOptions* opt, void* stream);
