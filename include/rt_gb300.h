@@ -242,9 +242,15 @@ rt_status rt_build_bvh_device(const RtTriangle64* d_triangles, uint32_t num_tria
 enum {
   RT_TRACE_CLOSEST = 0,  /* closest hit in [tmin, tmax] (hitBVH, raytraceBVH.comp:195-265) */
   RT_TRACE_ANY = 1,      /* any hit in [tmin, tmax] (occlusion) */
-  RT_TRACE_SORT = 2      /* or'ed in: trace the batch in an order bucketed by ray origin
+  RT_TRACE_SORT = 2,     /* or'ed in: trace the batch in an order bucketed by ray origin
                             (coherence); hits are unchanged and still land in ray order.
-                            Uses a per-stream device workspace of about 6 bytes per ray. */
+                            Uses a per-stream device workspace of about 10 bytes per ray. */
+  RT_TRACE_MT = 4        /* or'ed in (rt_trace, rt_trace_host): the Moller-Trumbore
+                            ray-triangle test (J. Graphics Tools 2(1), 1997) in binary32
+                            instead of the reference's plane test (raytraceBVH.comp:118-149).
+                            Not the reference's arithmetic: it also hits rays within
+                            |n.d| < 1e-4 of the plane, which the reference rejects, and
+                            its t and edge decisions round differently. */
 };
 
 /* Traces n rays resident on the device; writes n hits.  Stream-ordered. */

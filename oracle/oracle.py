@@ -118,12 +118,15 @@ def build_bvh(tris, spheres=None, mode: int = 0, models=None):
     return nodes, codes, prims, enc
 
 
-def trace(scene: Scene, rays, any_hit: bool = False, canonical: bool = False, nthreads: int | None = None):
-    """-> (hits, stats[5]: boxes, tris, spheres, inner, status)"""
+def trace(scene: Scene, rays, any_hit: bool = False, canonical: bool = False, nthreads: int | None = None,
+          mt: bool = False):
+    """-> (hits, stats[5]: boxes, tris, spheres, inner, status).  mt: the
+    Moller-Trumbore triangle test (the library's RT_TRACE_MT) instead of the
+    reference's plane test."""
     rays = np.ascontiguousarray(rays, dtype=RAY)
     hits = np.zeros(len(rays), HIT)
     stats = np.zeros(5, np.uint64)
-    flags = (1 if any_hit else 0) | (2 if canonical else 0)
+    flags = (1 if any_hit else 0) | (2 if canonical else 0) | (4 if mt else 0)
     lib().orc_trace(C.byref(scene.s), _p(rays), len(rays), _p(hits), flags,
                     nthreads if nthreads is not None else threads(), _p(stats))
     return hits, stats

@@ -286,6 +286,36 @@ static int triangle_hit(const OTri* T, v3 o, v3 d, float tmin, float tmax, ORec*
   return 1;
 }
 
+/* Not the reference's test: Moller & Trumbore, "Fast, minimum storage
+ * ray-triangle intersection", J. Graphics Tools 2(1), 1997, in binary32
+ * under the contract above (the library's RT_TRACE_MT mode):
+ *   e1 = v1 - v0, e2 = v2 - v0, p = cross(d, e2), det = dot(e1, p)
+ *   (det == 0: parallel, a miss), s = o - v0, u = dot(s, p) * (1/det),
+ *   q = cross(s, e1), v = dot(d, q) * (1/det), t = dot(e2, q) * (1/det);
+ *   a hit when 0 <= u <= 1, v >= 0, u + v <= 1 and tmin <= t <= tmax. */
+static int triangle_hit_mt(const OTri* T, v3 o, v3 d, float tmin, float tmax, ORec* rec) {
+  v3 v0 = V4(T->v0), v1 = V4(T->v1), v2 = V4(T->v2);
+  v3 e1 = vsub(v1, v0);
+  v3 e2 = vsub(v2, v0);
+  v3 p = vcross(d, e2);
+  float det = vdot(e1, p);
+  if (!(fabsf(det) > 0.0f)) return 0;
+  float inv = 1.0f / det;
+  v3 s = vsub(o, v0);
+  float u = vdot(s, p) * inv;
+  if (!(u >= 0.0f && u <= 1.0f)) return 0;
+  v3 q = vcross(s, e1);
+  float v = vdot(d, q) * inv;
+  if (!(v >= 0.0f && u + v <= 1.0f)) return 0;
+  float t = vdot(e2, q) * inv;
+  if (!(t >= tmin && t <= tmax)) return 0;
+  rec->t = t;
+  rec->u = u;
+  rec->v = v;
+  rec->mat = T->mat;
+  return 1;
+}
+
 /* raytraceBVH.comp:152-181 (u,v of :172-173 are never read on the path) */
 static int sphere_hit(const OSph* S, v3 o, v3 d, float tmin, float tmax, ORec* rec) {
   v3 C = V4(S->c);
@@ -331,7 +361,7 @@ typedef struct {
 } OStats;
 
 static int leaf_test(const OScene* S, const ONode* nd, v3 o, v3 d, float tmin, float closest,
-                     ORec* rec, OStats* st) {
+                     ORec* rec, OStats* st, int mt) {
   if (nd->ptype == SPHERE_PRIMITIVE) {
     if (nd->prim >= S->ns) { st->status |= 2; return 0; }
     st->spheres++;
@@ -342,7 +372,8 @@ static int leaf_test(const OScene* S, const ONode* nd, v3 o, v3 d, float tmin, f
   } else if (nd->ptype == TRIANGLE_PRIMITIVE) {
     if (nd->prim >= S->nt) { st->status |= 2; return 0; }
     st->tris++;
-    if (triangle_hit(&S->tris[nd->prim], o, d, tmin, closest, rec)) {
+    if (mt ? triangle_hit_mt(&S->tris[nd->prim], o, d, tmin, closest, rec)
+           : triangle_hit(&S->tris[nd->prim], o, d, tmin, closest, rec)) {
       rec->prim = nd->prim;
       return 1;
     }
@@ -355,7 +386,7 @@ static int leaf_test(const OScene* S, const ONode* nd, v3 o, v3 d, float tmin, f
  * pushes its left child and continues with its right child; no interval
  * culling; a later candidate at equal t replaces the earlier one. */
 static int hit_bvh_reference(const OScene* S, v3 o, v3 d, float tmin, float tmax, int any,
-                             ORec* rec, OStats* st) {
+                             ORec* rec, OStats* st, int mt) {
   if (S->nn == 0) return 0;
   int hit = 0;
   float closest = tmax;
@@ -369,7 +400,7 @@ static int hit_bvh_reference(const OScene* S, v3 o, v3 d, float tmin, float tmax
     slab(o, d, nd, &tn, &tf);
     if (tn < tf) {
       if (nd->left == 0u && nd->right == 0u) {
-        if (leaf_test(S, nd, o, d, tmin, closest, rec, st)) {
+        if (leaf_test(S, nd, o, d, tmin, closest, rec, st, mt)) {
           hit = 1;
           closest = rec->t;
           if (any) break;
@@ -396,7 +427,7 @@ static int hit_bvh_reference(const OScene* S, v3 o, v3 d, float tmin, float tmax
  * far above binary32 rounding of t.  It returns the reference's answer except
  * on exact ties of t, which the reference breaks by visit order. */
 static int hit_bvh_canonical(const OScene* S, v3 o, v3 d, float tmin, float tmax, int any,
-                             ORec* rec, OStats* st) {
+                             ORec* rec, OStats* st, int mt) {
   if (S->nn == 0) return 0;
   int hit = 0;
   float closest = tmax;
@@ -414,7 +445,7 @@ static int hit_bvh_canonical(const OScene* S, v3 o, v3 d, float tmin, float tmax
     const ONode* nd = &S->nodes[cur];
     int next_valid = 0;
     if (nd->left == 0u && nd->right == 0u) {
-      if (leaf_test(S, nd, o, d, tmin, closest, rec, st)) {
+      if (leaf_test(S, nd, o, d, tmin, closest, rec, st, mt)) {
         hit = 1;
         closest = rec->t;
         if (any) break;
@@ -458,18 +489,18 @@ typedef struct {
   const ORay* rays;
   OHit* hits;
   uint32_t n;
-  int any, canonical;
+  int any, canonical, mt;
   _Atomic uint32_t next;
   OStats totals;
   pthread_mutex_t lock;
 } TraceJob;
 
-static void trace_one(const OScene* S, const ORay* r, OHit* h, int any, int canonical, OStats* st) {
+static void trace_one(const OScene* S, const ORay* r, OHit* h, int any, int canonical, int mt, OStats* st) {
   ORec rec;
   memset(&rec, 0, sizeof(rec));
   v3 o = V(r->o[0], r->o[1], r->o[2]), d = V(r->d[0], r->d[1], r->d[2]);
-  int hit = canonical ? hit_bvh_canonical(S, o, d, r->tmin, r->tmax, any, &rec, st)
-                      : hit_bvh_reference(S, o, d, r->tmin, r->tmax, any, &rec, st);
+  int hit = canonical ? hit_bvh_canonical(S, o, d, r->tmin, r->tmax, any, &rec, st, mt)
+                      : hit_bvh_reference(S, o, d, r->tmin, r->tmax, any, &rec, st, mt);
   if (hit) { h->prim = rec.prim; h->t = rec.t; }
   else { h->prim = NO_HIT; h->t = INFINITY; }
 }
@@ -482,7 +513,7 @@ static void* trace_worker(void* arg) {
     uint32_t b = atomic_fetch_add(&J->next, 64u);
     if (b >= J->n) break;
     uint32_t e = b + 64u < J->n ? b + 64u : J->n;
-    for (uint32_t i = b; i < e; ++i) trace_one(J->S, &J->rays[i], &J->hits[i], J->any, J->canonical, &st);
+    for (uint32_t i = b; i < e; ++i) trace_one(J->S, &J->rays[i], &J->hits[i], J->any, J->canonical, J->mt, &st);
   }
   pthread_mutex_lock(&J->lock);
   J->totals.boxes += st.boxes; J->totals.tris += st.tris; J->totals.spheres += st.spheres;
@@ -492,13 +523,14 @@ static void* trace_worker(void* arg) {
 }
 
 /* Traces n rays.  flags bit0 = any-hit, bit1 = canonical order (else the
- * reference order).  stats (may be NULL) receives the OStats totals. */
+ * reference order), bit2 = the Moller-Trumbore triangle test (else the
+ * reference's plane test).  stats (may be NULL) receives the OStats totals. */
 int orc_trace(const OScene* S, const ORay* rays, uint32_t n, OHit* hits, uint32_t flags,
               uint32_t nthreads, uint64_t* stats) {
   TraceJob J;
   memset(&J, 0, sizeof(J));
   J.S = S; J.rays = rays; J.hits = hits; J.n = n;
-  J.any = (flags & 1u) != 0; J.canonical = (flags & 2u) != 0;
+  J.any = (flags & 1u) != 0; J.canonical = (flags & 2u) != 0; J.mt = (flags & 4u) != 0;
   atomic_init(&J.next, 0u);
   pthread_mutex_init(&J.lock, NULL);
   if (nthreads <= 1) {
@@ -626,7 +658,7 @@ static v3 ray_color(const OScene* S, v3 o, v3 d, uint32_t depth, uint32_t* rng, 
   for (uint32_t i = 0; i < depth; ++i) {
     ORec rec;
     memset(&rec, 0, sizeof(rec));
-    if (!hit_bvh_reference(S, co, cd, 0.001f, 10000000.0f, 0, &rec, st)) {
+    if (!hit_bvh_reference(S, co, cd, 0.001f, 10000000.0f, 0, &rec, st, 0)) {
       v3 b = extended ? bg : V(0.0f, 0.0f, 0.0f);
       color = vadd(color, vmul(b, gatt));
       break;

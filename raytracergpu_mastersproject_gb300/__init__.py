@@ -44,7 +44,7 @@ assert NODE_DTYPE.itemsize == 40 and RAY_DTYPE.itemsize == 32 and HIT_DTYPE.item
 MAT_LIGHT, MAT_DIFFUSE, MAT_METALLIC, MAT_DIELECTRIC = 0, 1, 2, 3
 PRIM_SPHERE, PRIM_TRIANGLE = 0, 1
 BVH_SORTED, BVH_REFERENCE = 0, 1
-TRACE_CLOSEST, TRACE_ANY, TRACE_SORT = 0, 1, 2
+TRACE_CLOSEST, TRACE_ANY, TRACE_SORT, TRACE_MT = 0, 1, 2, 4
 SHADE_REFERENCE, SHADE_EXTENDED = 0, 1
 NO_HIT = 0xFFFFFFFF
 HIT_SPHERE_BIT = 0x80000000
@@ -288,12 +288,14 @@ class Scene:
         _check(lib().rt_scene_get_nodes(self.handle, _ptr(out), n), "rt_scene_get_nodes")
         return out
 
-    def trace(self, rays, hits, n: int | None = None, any_hit: bool = False, sort: bool = False, stream=None) -> None:
+    def trace(self, rays, hits, n: int | None = None, any_hit: bool = False, sort: bool = False, stream=None,
+              mt: bool = False) -> None:
         """rays/hits: device tensors holding RtRay / RtHit records (stream-ordered).
-        sort: trace in an origin-bucketed order for coherence (same results)."""
+        sort: trace in an origin-bucketed order for coherence (same results).
+        mt: the Moller-Trumbore triangle test instead of the reference's plane test."""
         if n is None:
             n = rays.numel() * rays.element_size() // RAY_DTYPE.itemsize
-        flags = (TRACE_ANY if any_hit else TRACE_CLOSEST) | (TRACE_SORT if sort else 0)
+        flags = (TRACE_ANY if any_hit else TRACE_CLOSEST) | (TRACE_SORT if sort else 0) | (TRACE_MT if mt else 0)
         _check(lib().rt_trace(self.handle, _ptr(rays), n, _ptr(hits), flags, _stream_handle(stream)), "rt_trace")
 
     def trace_count(self, rays, hits, n: int | None = None, any_hit: bool = False, sort: bool = False,
@@ -308,12 +310,12 @@ class Scene:
         return int(c[0]), int(c[1])
 
     def trace_host(self, rays: np.ndarray, any_hit: bool = False, out: np.ndarray | None = None, sort: bool = False,
-                   stream=None) -> np.ndarray:
+                   stream=None, mt: bool = False) -> np.ndarray:
         """Host rays in, host hits out; copies overlap with tracing inside the library."""
         rays = np.ascontiguousarray(rays, dtype=RAY_DTYPE)
         if out is None:
             out = np.empty(len(rays), HIT_DTYPE)
-        flags = (TRACE_ANY if any_hit else TRACE_CLOSEST) | (TRACE_SORT if sort else 0)
+        flags = (TRACE_ANY if any_hit else TRACE_CLOSEST) | (TRACE_SORT if sort else 0) | (TRACE_MT if mt else 0)
         _check(lib().rt_trace_host(self.handle, _ptr(rays), len(rays), _ptr(out), flags, _stream_handle(stream)),
                "rt_trace_host")
         return out

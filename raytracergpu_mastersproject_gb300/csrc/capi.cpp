@@ -484,7 +484,8 @@ rt_status rt_scene_get_nodes(const rt_scene* scene, RtBVHNode40* h_out, uint32_t
 
 rt_status rt_trace(rt_scene* scene, const RtRay* d_rays, uint32_t n, RtHit* d_hits, uint32_t flags, void* stream) {
   rtgb::NvtxRange nvtx_range("rt_trace");
-  if (!scene || (n && (!d_rays || !d_hits)) || flags > (RT_TRACE_ANY | RT_TRACE_SORT) || n > 0x80000000u) {
+  if (!scene || (n && (!d_rays || !d_hits)) || flags > (RT_TRACE_ANY | RT_TRACE_SORT | RT_TRACE_MT) ||
+      n > 0x80000000u) {
     set_error("rt_trace: bad argument");
     return RT_EINVAL;
   }
@@ -535,7 +536,8 @@ rt_status rt_trace_count(rt_scene* scene, const RtRay* d_rays, uint32_t n, RtHit
 rt_status rt_trace_host(rt_scene* scene, const RtRay* h_rays, uint32_t n, RtHit* h_hits, uint32_t flags,
                         void* stream) {
   rtgb::NvtxRange nvtx_range("rt_trace_host");
-  if (!scene || (n && (!h_rays || !h_hits)) || flags > (RT_TRACE_ANY | RT_TRACE_SORT) || n > 0x80000000u) {
+  if (!scene || (n && (!h_rays || !h_hits)) || flags > (RT_TRACE_ANY | RT_TRACE_SORT | RT_TRACE_MT) ||
+      n > 0x80000000u) {
     set_error("rt_trace_host: bad argument");
     return RT_EINVAL;
   }

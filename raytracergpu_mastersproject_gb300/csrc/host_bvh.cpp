@@ -329,7 +329,7 @@ void build_bvh(const RtTriangle64* tris, uint32_t nt, const RtSphere32* sph, uin
 // ------------------------------------------------ SAH traversal tree ----
 // A binned surface-area-heuristic tree over the same primitives, in the node
 // form convert_bvh reads (root 0, leaves with left == right == 0, one
-// primitive per leaf).  Used for traversal only: closest hits do not depend
+// primitive per leaf, no leaf box flat).  Used for traversal only: closest hits do not depend
 // on the tree, and the scene keeps the reference-layout nodes for export.
 //
 // Primitive records (bounds, centroid, id) are kept in tree order and
@@ -610,11 +610,21 @@ void build_sah(const RtTriangle64* tris, uint32_t nt, const RtSphere32* sph, uin
       } else {
         const RtSphere32& S = sph[i - nt];
         for (int a = 0; a < 3; ++a) {
-          r.lo[a] = S.center[a] - S.radius;
-          r.hi[a] = S.center[a] + S.radius;
+          const float l = S.center[a] - S.radius, h = S.center[a] + S.radius;
+          r.lo[a] = std::fmin(l, h);
+          r.hi[a] = std::fmax(l, h);
         }
       }
       for (int a = 0; a < 3; ++a) r.c[a] = 0.5f * r.lo[a] + 0.5f * r.hi[a];
+      // An exactly flat axis (an axis-aligned triangle) gets 2^-20 of its
+      // magnitude on each side, so that a strict slab test (tNear < tFar)
+      // can enter the box; no other box is changed.
+      for (int a = 0; a < 3; ++a)
+        if (r.hi[a] == r.lo[a]) {
+          const float e = std::fmax(std::fabs(r.lo[a]), 1e-30f) * 9.5367431640625e-07f;
+          r.lo[a] -= e;
+          r.hi[a] += e;
+        }
       r.id = (uint32_t)i;
     }
   });

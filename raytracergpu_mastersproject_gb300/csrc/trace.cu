@@ -31,7 +31,7 @@ __device__ __forceinline__ uint32_t lanemask_lt() {
 // THREADS per block and MINB resident blocks per SM (the register cap) are
 // launch-shape knobs; `refill` is the lane count below which a warp stops to
 // hand new rays to its idle lanes (0: only when all lanes are idle).
-template <bool ANY, int STACK, int THREADS, int MINB, int W, bool STATS>
+template <bool ANY, int STACK, int THREADS, int MINB, int W, bool STATS, bool MT = false>
 __global__ void __launch_bounds__(THREADS, MINB)
     k_trace(DeviceScene S, const float4* __restrict__ rays, uint32_t n, uint2* __restrict__ hits,
             uint32_t* __restrict__ counter, int refill, unsigned long long* __restrict__ stats,
@@ -68,7 +68,7 @@ __global__ void __launch_bounds__(THREADS, MINB)
     if (ray != 0xFFFFFFFFu) {
       bool done;
       if constexpr (W == 2)
-        done = dev::trav_run<ANY, STACK>(S, s, stack, exhausted ? 0 : refill);
+        done = dev::trav_run<ANY, STACK, MT>(S, s, stack, exhausted ? 0 : refill);
       else
         done = dev::trav_run_wide<ANY, STACK>(S, s, stack, exhausted ? 0 : refill);
       if (done || s.sp < 0) {
@@ -119,7 +119,7 @@ __global__ void __launch_bounds__(THREADS, MINB)
 //
 // RING > 0 keeps the top RING stack entries of each lane in shared memory
 // (RING * THREADS * 8 bytes per block), the rest in local memory.
-template <bool ANY, int STACK, int THREADS, int MINB, bool STATS, bool RAW = false, int RING = 0>
+template <bool ANY, int STACK, int THREADS, int MINB, bool STATS, bool RAW = false, int RING = 0, bool MT = false>
 __global__ void __launch_bounds__(THREADS, MINB)
     k_trace_step(DeviceScene S, const float4* __restrict__ rays, uint32_t n, uint2* __restrict__ hits,
                  uint32_t* __restrict__ counter, int refill, unsigned long long* __restrict__ stats,
@@ -172,7 +172,7 @@ __global__ void __launch_bounds__(THREADS, MINB)
       if (!dev::visit_wide_stk<STACK>(S, s, stk)) done = true;
     }
     if (!done && dev::is_leaf(s.node)) {
-      if (dev::leaf_visit<ANY>(S, s, s.node))
+      if (dev::leaf_visit<ANY, MT>(S, s, s.node))
         done = true;
       else
         s.node = stk.pop(s);
@@ -273,6 +273,21 @@ Variant g_variants[] = {make_variant<128, 12, false>(), make_variant<128, 10, fa
                         make_variant<128, 10, true, 16>(), make_variant<256, 5, true, 16>()};
 constexpr int kNumVariants = sizeof(g_variants) / sizeof(g_variants[0]);
 
+// RT_TRACE_MT: the Moller-Trumbore leaf test in the default launch shape (the
+// step loop with the shared ring for 4-wide trees, the while-while loop for
+// binary ones), 128 threads x 10 blocks.  [wide][any][big stack]
+struct MtKernels {
+  TraceKernel k[2][2][2];
+  int blocks_per_sm[2][2][2];
+};
+MtKernels g_mt = {{{{k_trace<false, 64, 128, 10, 2, false, true>, k_trace<false, 128, 128, 10, 2, false, true>},
+                    {k_trace<true, 64, 128, 10, 2, false, true>, k_trace<true, 128, 128, 10, 2, false, true>}},
+                   {{k_trace_step<false, 64, 128, 10, false, false, 16, true>,
+                     k_trace_step<false, 192, 128, 10, false, false, 16, true>},
+                    {k_trace_step<true, 64, 128, 10, false, false, 16, true>,
+                     k_trace_step<true, 192, 128, 10, false, false, 16, true>}}},
+                  {{{-1, -1}, {-1, -1}}, {{-1, -1}, {-1, -1}}}};
+
 int env_int(const char* name, int dflt) {
   const char* e = std::getenv(name);
   return e ? std::atoi(e) : dflt;
@@ -306,18 +321,20 @@ cudaError_t launch_trace_tuned(const DeviceScene& S, const RtRay* rays, uint32_t
   const int wide = S.width == 4 ? 1 : 0;
   const int big = S.stack_need > 64u ? 1 : 0;
   const int st = stats ? 1 : 0;
-  TraceKernel k = v.k[st][wide][any][big];
+  const bool mt = (flags & RT_TRACE_MT) != 0;
+  if (mt && stats) return cudaErrorInvalidValue;  // no counting instantiation of the MT test
+  TraceKernel k = mt ? g_mt.k[wide][any][big] : v.k[st][wide][any][big];
+  const int threads = mt ? 128 : v.threads;
+  int* slot = mt ? &g_mt.blocks_per_sm[wide][any][big] : &v.blocks_per_sm[st][wide][any][big];
   int bps = 0;
-  if (cudaError_t e = cached_blocks_per_sm(&v.blocks_per_sm[st][wide][any][big], k, v.threads, &bps);
-      e != cudaSuccess)
-    return e;
-  const uint32_t warps_per_block = (uint32_t)v.threads / 32u;
+  if (cudaError_t e = cached_blocks_per_sm(slot, k, threads, &bps); e != cudaSuccess) return e;
+  const uint32_t warps_per_block = (uint32_t)threads / 32u;
   const uint32_t warps_needed = (n + 31u) / 32u;
   uint64_t blocks = (uint64_t)device_sm_count() * (uint64_t)bps * (uint64_t)std::max(1, tune.grid_scale) / 100u;
   const uint64_t needed = (warps_needed + warps_per_block - 1) / warps_per_block;
   if (blocks > needed) blocks = needed;
   if (blocks == 0) blocks = 1;
-  k<<<(uint32_t)blocks, v.threads, 0, reinterpret_cast<cudaStream_t>(stream)>>>(
+  k<<<(uint32_t)blocks, threads, 0, reinterpret_cast<cudaStream_t>(stream)>>>(
       S, reinterpret_cast<const float4*>(rays), n, reinterpret_cast<uint2*>(hits), counter, tune.refill, stats, order);
   return cudaGetLastError();
 }
@@ -379,7 +396,7 @@ extern "C" rt_status rt_trace_noalloc(rt_scene* scene, const RtRay* d_rays, uint
                                       uint32_t flags, void* stream) {
   rtgb::NvtxRange nvtx_range("rt_trace_noalloc");
   using namespace rtgb;
-  if (!scene || (n && (!d_rays || !d_hits)) || flags > RT_TRACE_ANY) {
+  if (!scene || (n && (!d_rays || !d_hits)) || (flags & ~(uint32_t)(RT_TRACE_ANY | RT_TRACE_MT))) {
     set_error("rt_trace_noalloc: bad argument");
     return RT_EINVAL;
   }

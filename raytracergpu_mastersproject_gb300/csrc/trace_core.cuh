@@ -51,6 +51,35 @@ __device__ __forceinline__ bool tri_test(const void* tris, uint32_t slot, float 
   return true;
 }
 
+// Moller & Trumbore, "Fast, minimum storage ray-triangle intersection",
+// J. Graphics Tools 2(1), 1997, on the same record (v0, e1 = v1 - v0,
+// e2 = v2 - v0) under the same arithmetic contract: p = d x e2,
+// det = e1 . p (0: the ray is parallel, a miss), u = (o - v0) . p / det,
+// q = (o - v0) x e1, v = d . q / det, t = e2 . q / det.  An optional mode
+// (RT_TRACE_MT), not the reference's test.
+__device__ __forceinline__ bool tri_test_mt(const void* tris, uint32_t slot, float ox, float oy, float oz,
+                                            float dx, float dy, float dz, float tmin, float tmax, float& t_out) {
+  const float4 r1 = ldg4(tris, 4u * slot + 1u);  // w.xyz, v0.x
+  const float4 r2 = ldg4(tris, 4u * slot + 2u);  // v0.y, v0.z, e1.x, e1.y
+  const float4 r3 = ldg4(tris, 4u * slot + 3u);  // e1.z, e2.x, e2.y, e2.z
+  const float e1x = r2.z, e1y = r2.w, e1z = r3.x;
+  const float e2x = r3.y, e2y = r3.z, e2z = r3.w;
+  const float px = dy * e2z - dz * e2y, py = dz * e2x - dx * e2z, pz = dx * e2y - dy * e2x;
+  const float det = e1x * px + e1y * py + e1z * pz;
+  if (!(fabsf(det) > 0.0f)) return false;  // parallel (or NaN)
+  const float inv = 1.0f / det;
+  const float tx = ox - r1.w, ty = oy - r2.x, tz = oz - r2.y;
+  const float u = (tx * px + ty * py + tz * pz) * inv;
+  if (!(u >= 0.0f && u <= 1.0f)) return false;
+  const float qx = ty * e1z - tz * e1y, qy = tz * e1x - tx * e1z, qz = tx * e1y - ty * e1x;
+  const float v = (dx * qx + dy * qy + dz * qz) * inv;
+  if (!(v >= 0.0f && u + v <= 1.0f)) return false;
+  const float t = (e2x * qx + e2y * qy + e2z * qz) * inv;
+  if (!(t >= tmin && t <= tmax)) return false;
+  t_out = t;
+  return true;
+}
+
 // sphereHit (raytraceBVH.comp:152-181) -- root only; the hit record is rebuilt
 // by the caller when it needs the normal.
 __device__ __forceinline__ bool sphere_test(const void* spheres, uint32_t idx, float ox, float oy, float oz,
@@ -177,8 +206,8 @@ __device__ __forceinline__ bool is_inner(uint32_t r) { return r < kSentinel; }
 __device__ __forceinline__ bool is_leaf(uint32_t r) { return r > kSentinel; }
 
 // Tests the primitives of one leaf ref; returns true when the ray is done
-// (any-hit found).
-template <bool ANY>
+// (any-hit found).  MT: the Moller-Trumbore triangle test (RT_TRACE_MT).
+template <bool ANY, bool MT = false>
 __device__ __forceinline__ bool leaf_visit(const DeviceScene& S, Trav& s, uint32_t leaf) {
   if (leaf & kSphereBit) {
     const uint32_t idx = leaf & kSphereMask;
@@ -198,7 +227,9 @@ __device__ __forceinline__ bool leaf_visit(const DeviceScene& S, Trav& s, uint32
   for (uint32_t k = 0; k < count; ++k) {
     float t;
     s.ntest++;
-    if (tri_test(S.tris, first + k, s.ox, s.oy, s.oz, s.dx, s.dy, s.dz, s.tmin, s.tclose, t)) {
+    const bool hit = MT ? tri_test_mt(S.tris, first + k, s.ox, s.oy, s.oz, s.dx, s.dy, s.dz, s.tmin, s.tclose, t)
+                        : tri_test(S.tris, first + k, s.ox, s.oy, s.oz, s.dx, s.dy, s.dz, s.tmin, s.tclose, t);
+    if (hit) {
       trav_set_close(s, t);
       s.best = kLeafBit | (first + k);
       if (ANY) return true;
@@ -211,7 +242,7 @@ __device__ __forceinline__ bool leaf_visit(const DeviceScene& S, Trav& s, uint32
 // false early when fewer than `refill` lanes of the warp are still traversing,
 // so that the warp can hand new rays to its idle lanes (state is kept).
 // Returns false with s.sp == -1 on stack overflow (the ray is abandoned).
-template <bool ANY, int STACK>
+template <bool ANY, int STACK, bool MT = false>
 __device__ __forceinline__ bool trav_run(const DeviceScene& S, Trav& s, uint32_t* stack, int refill) {
   for (;;) {
     // Inner nodes: descend, postponing the first leaf found.
@@ -259,7 +290,7 @@ __device__ __forceinline__ bool trav_run(const DeviceScene& S, Trav& s, uint32_t
     }
     // Leaves: test the postponed leaf, then any leaves popped in sequence.
     while (s.leaf != 0u) {
-      if (leaf_visit<ANY>(S, s, s.leaf)) {
+      if (leaf_visit<ANY, MT>(S, s, s.leaf)) {
         s.leaf = 0u;
         s.node = kSentinel;
         return true;

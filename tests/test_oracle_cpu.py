@@ -209,6 +209,112 @@ def test_any_hit_reports_a_real_hit(rt, orc):
         assert t is not None and np.float32(t) == a["t"][i] and a["t"][i] >= c["t"][i]
 
 
+# ------------------------------------------------- Moller-Trumbore mode ----
+def _mt_numpy(tris, ray):
+    """Moller-Trumbore in numpy binary32 (one rounding per operation, the
+    oracle's evaluation order) against every triangle -> (t per triangle, hit mask)."""
+    f = np.float32
+    v0, v1, v2 = (tris[k][:, :3].astype(f) for k in ("v0", "v1", "v2"))
+    o, d = ray["org"][0].astype(f), ray["dir"][0].astype(f)
+    e1, e2 = v1 - v0, v2 - v0
+    px = d[1] * e2[:, 2] - d[2] * e2[:, 1]
+    py = d[2] * e2[:, 0] - d[0] * e2[:, 2]
+    pz = d[0] * e2[:, 1] - d[1] * e2[:, 0]
+    det = (e1[:, 0] * px + e1[:, 1] * py) + e1[:, 2] * pz
+    with np.errstate(divide="ignore", invalid="ignore"):
+        inv = f(1.0) / det
+        s = o - v0
+        u = ((s[:, 0] * px + s[:, 1] * py) + s[:, 2] * pz) * inv
+        qx = s[:, 1] * e1[:, 2] - s[:, 2] * e1[:, 1]
+        qy = s[:, 2] * e1[:, 0] - s[:, 0] * e1[:, 2]
+        qz = s[:, 0] * e1[:, 1] - s[:, 1] * e1[:, 0]
+        v = ((d[0] * qx + d[1] * qy) + d[2] * qz) * inv
+        t = ((e2[:, 0] * qx + e2[:, 1] * qy) + e2[:, 2] * qz) * inv
+        ok = (np.abs(det) > 0) & (u >= 0) & (u <= 1) & (v >= 0) & (u + v <= 1)
+        ok &= (t >= ray["tmin"][0]) & (t <= ray["tmax"][0])
+    return t, ok
+
+
+def test_mt_restatement_matches_numpy(rt, orc):
+    """The oracle's Moller-Trumbore mode against an independent numpy
+    binary32 restatement over every triangle: the same closest t bit for bit
+    (the same id unless another triangle has exactly that t)."""
+    soup = rt.gen_soup(21, 0, 3_000, 1.0, 0.02)
+    rays = rt.gen_rays(21, 0, 400, 1.0, 1e-4, float("inf"))
+    nodes, _, _, _ = orc.build_bvh(soup, mode=0)
+    got, _ = orc.trace(orc.Scene(soup, nodes), rays, mt=True)
+    hits = 0
+    for i in range(len(rays)):
+        t, ok = _mt_numpy(soup, rays[i:i + 1])
+        if not ok.any():
+            assert got["prim"][i] == orc.NO_HIT
+            continue
+        hits += 1
+        tmin = t[ok].min()
+        assert got["prim"][i] != orc.NO_HIT and got["t"][i].view(np.uint32) == np.float32(tmin).view(np.uint32)
+        assert t[got["prim"][i]] == tmin and ok[got["prim"][i]]
+    assert hits > 100
+
+
+def _mt_explained(tri, ray, t_mt, t_plane, extent):
+    """Why a Moller-Trumbore hit can differ from the plane test's: the ray
+    grazes the plane (|n.d| < 1e-4, rejected by the reference), the hit lies on
+    an edge (a barycentric within 1e-5 of 0, or u+v of 1, in binary64), or the
+    two answers are a near-tie in t."""
+    v0, v1, v2 = (tri[k][:3].astype(np.float64) for k in ("v0", "v1", "v2"))
+    o, d = ray["org"][0].astype(np.float64), ray["dir"][0].astype(np.float64)
+    n = np.cross(v1 - v0, v2 - v0)
+    if np.linalg.norm(n) == 0:
+        return "degenerate"
+    n /= np.linalg.norm(n)
+    if abs(n @ d) < 1.01e-4:
+        return "grazing"
+    t = ((v0 - o) @ n) / (n @ d)
+    p = o + t * d
+    e1, e2, q = v1 - v0, v2 - v0, p - v0
+    m = np.array([[e1 @ e1, e1 @ e2], [e1 @ e2, e2 @ e2]])
+    u, v = np.linalg.solve(m, np.array([q @ e1, q @ e2]))
+    if min(abs(u), abs(v), abs(1 - u - v)) < 1e-5:
+        return "edge"
+    if np.isfinite(t_plane) and abs(t_mt - t_plane) <= 1e-5 * max(abs(t_mt), extent):
+        return "near-tie"
+    return None
+
+
+def test_mt_divergence_set(rt, orc):
+    """The Moller-Trumbore mode against the reference's plane test: hit ids
+    agree except on grazing rays, edge hits and near-ties; matching hits agree
+    in t within 1e-5 of max(t, scene extent) (the plane test's t cancels for
+    hits near the ray origin)."""
+    cases = []
+    tris, _, rays = rt.gen_config1()
+    cases.append((tris, rays[::3], 20.0))
+    soup = rt.gen_soup(22, 0, 50_000, 1.0, 0.004)
+    cases.append((soup, rt.gen_rays(22, 0, 20_000, 1.0, 1e-4, float("inf")), 1.0))
+    for tris, rays, extent in cases:
+        nodes, _, _, _ = orc.build_bvh(tris, mode=0)
+        S = orc.Scene(tris, nodes)
+        plane, _ = orc.trace(S, rays, canonical=True)
+        mt, _ = orc.trace(S, rays, canonical=True, mt=True)
+        same = plane["prim"] == mt["prim"]
+        both = same & (plane["prim"] != orc.NO_HIT)
+        assert both.sum() > 0.1 * len(rays)
+        dt = np.abs(plane["t"][both].astype(np.float64) - mt["t"][both])
+        assert np.all(dt <= 1e-5 * np.maximum(np.abs(mt["t"][both]), extent))
+        diff = np.nonzero(~same)[0]
+        assert len(diff) <= 0.01 * len(rays)
+        for i in diff:
+            r = rays[i:i + 1]
+            if mt["prim"][i] == orc.NO_HIT:  # the plane test hit where MT missed: an edge or near-tie
+                why = _mt_explained(tris[plane["prim"][i]], r, np.inf, plane["t"][i], extent) or "mt-miss"
+                assert why in ("edge", "grazing", "degenerate"), (i, why)
+                continue
+            why = _mt_explained(tris[mt["prim"][i]], r, mt["t"][i], plane["t"][i], extent)
+            if why is None and plane["prim"][i] != orc.NO_HIT:
+                why = _mt_explained(tris[plane["prim"][i]], r, mt["t"][i], plane["t"][i], extent)
+            assert why is not None, (i, mt[i], plane[i])
+
+
 def test_resolve_formula(orc):
     acc = np.array([0.0, 0.25, 4.0, 1.0, -1.0, 1e-8, 2.0, 0.5], np.float32)
     out = orc.resolve(acc, 2, 1, 4)

@@ -82,3 +82,22 @@ def test_sah_tiny_inputs(rt, n):
     assert len(nodes) == max(2 * n - 1, 0)
     if n == 1:
         assert nodes[0]["left"] == 0 and nodes[0]["right"] == 0 and nodes[0]["primitiveType"] == rt.PRIM_TRIANGLE
+
+
+def test_sah_flat_leaves_are_widened(rt, orc):
+    """An axis-aligned quad has a flat box; the reference pads such leaf boxes
+    (ConstructHLBVH.comp:38-54) so that its strict slab test can enter them.
+    The SAH tree widens exactly flat axes by 2^-20 of their magnitude: config
+    1's ground quad is hit through it exactly as through the S1 tree through
+    the oracle's strict test, and no SAH box is flat."""
+    tris, _, rays = rt.gen_config1()
+    sah = rt.build_bvh_sah(tris)
+    s1, _, _, _ = orc.build_bvh(tris, mode=0)
+    for ax in ("X", "Y", "Z"):
+        assert np.all(sah["max" + ax] - sah["min" + ax] > 0)
+    a, _ = orc.trace(orc.Scene(tris, s1), rays[::5], canonical=True)
+    b, _ = orc.trace(orc.Scene(tris, sah), rays[::5], canonical=True)
+    assert np.array_equal(a["prim"], b["prim"])
+    assert np.array_equal(a["t"].view(np.uint32), b["t"].view(np.uint32))
+    ground = len(tris) - 2
+    assert (a["prim"] >= ground).sum() > 1000
