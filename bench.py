@@ -293,9 +293,11 @@ def run_batched(torch, rt) -> dict:
 
 
 def run_extras(torch, rt, scene, tris, d_rays, n: int) -> dict:
-    """Config 3 any-hit, the BVH build on host vs device, config 1 closest-hit."""
+    """Config 3 any-hit and Moller-Trumbore closest-hit, the BVH build on host
+    vs device, config 1 closest-hit."""
     d_hits = torch.empty(n * 8, dtype=torch.uint8, device="cuda")
     ms_any = _time_events(torch, lambda: scene.trace(d_rays, d_hits, any_hit=True, sort=True), warmup=2, reps=10)
+    ms_mt = _time_events(torch, lambda: scene.trace(d_rays, d_hits, sort=True, mt=True), warmup=2, reps=10)
     t0 = time.perf_counter()
     rt.build_bvh(tris)
     host_s = time.perf_counter() - t0
@@ -304,6 +306,9 @@ def run_extras(torch, rt, scene, tris, d_rays, n: int) -> dict:
     ms_dev = _time_events(torch, lambda: rt.build_bvh_device(d_t, len(tris), None, 0, d_n), warmup=1, reps=5)
     c1_tris, _, c1_rays = rt.gen_config1()
     out = {"config3_any_hit": {"value": n / ms_any / 1e6, "unit": UNIT, "ms": ms_any},
+           "config3_closest_hit_moller_trumbore": {
+               "value": n / ms_mt / 1e6, "unit": UNIT, "ms": ms_mt,
+               "note": "RT_TRACE_MT: not the reference's plane test; ids differ on edge hits (about 1 ray in 12,000)"},
            "bvh_build_config3": {"host_s": host_s, "host_threads": os.cpu_count(), "device_ms": ms_dev,
                                  "note": "2N-1 reference-layout nodes, identical bytes from both builders"}}
     with rt.Scene(c1_tris, bvh_mode=rt.BVH_REFERENCE) as s1:

@@ -5,6 +5,8 @@ The oracle restates hitBVH (raytraceBVH.comp:195-265) and triangleHit
 binary64 arbiter (oracle.arbitrate) accepts; matching hits must carry the
 bit-identical binary32 t.
 """
+import ctypes as C
+
 import numpy as np
 import pytest
 
@@ -461,3 +463,62 @@ def test_degenerate_rays(rt, orc, cuda):
     # NaN tmax behaves as +inf: the same hits as the unmodified rays
     base_hits = dev_trace(rt, cuda, rt.Scene(tris, node_width=4), base)
     assert np.array_equal(got4[7 * k:].view(np.uint64), base_hits.view(np.uint64))
+
+
+def assert_mt_parity(orc, ref, got):
+    """Moller-Trumbore results against the oracle's MT mode: ids equal except
+    where both answers have the same t within 1e-6 (a near-tie); matching
+    hits carry the bit-identical binary32 t."""
+    diff = np.nonzero(ref["prim"] != got["prim"])[0]
+    for i in diff:
+        a, b = float(ref["t"][i]), float(got["t"][i])
+        assert ref["prim"][i] != orc.NO_HIT and got["prim"][i] != orc.NO_HIT, (i, ref[i], got[i])
+        assert abs(a - b) <= 1e-6 * abs(a), (i, ref[i], got[i])
+    same = (ref["prim"] == got["prim"]) & (ref["prim"] != orc.NO_HIT)
+    assert np.array_equal(ref["t"][same].view(np.uint32), got["t"][same].view(np.uint32))
+    return len(diff)
+
+
+@pytest.mark.parametrize("width", [2, 4])
+def test_mt_mode_matches_oracle(rt, orc, cuda, width):
+    """RT_TRACE_MT against the oracle's Moller-Trumbore restatement: config 1
+    and a soup, closest hit (plain, sorted, host buffers) and any hit."""
+    tris, _, rays = rt.gen_config1()
+    soup = rt.gen_soup(31, 0, 200_000, 1.0, 0.004)
+    srays = rt.gen_rays(31, 0, 200_000, 1.0, 1e-4, float("inf"))
+    for t, r in ((tris, rays), (soup, srays)):
+        with rt.Scene(t, node_width=width) as sc:
+            assert sc.info().node_width == width
+            d_rays = cuda.from_numpy(np.ascontiguousarray(r).view(np.uint8)).cuda()
+            d_hits = cuda.empty(len(r) * 8, dtype=cuda.uint8, device="cuda")
+            sc.trace(d_rays, d_hits, mt=True)
+            cuda.cuda.synchronize()
+            got = d_hits.cpu().numpy().view(rt.HIT_DTYPE).copy()
+            sc.trace(d_rays, d_hits, mt=True, sort=True)
+            cuda.cuda.synchronize()
+            again = d_hits.cpu().numpy().view(rt.HIT_DTYPE).copy()
+            host = sc.trace_host(r, mt=True, sort=True)
+            sc.trace(d_rays, d_hits, mt=True, any_hit=True)
+            cuda.cuda.synchronize()
+            anyh = d_hits.cpu().numpy().view(rt.HIT_DTYPE).copy()
+            ref, st = orc.trace(orc.Scene(t, sc.nodes()), r, canonical=True, mt=True)
+        assert st[4] == 0
+        assert (ref["prim"] != orc.NO_HIT).sum() > 0.1 * len(r)
+        assert assert_mt_parity(orc, ref, got) <= 0.001 * len(r)
+        assert np.array_equal(got.view(np.uint64), again.view(np.uint64))
+        assert np.array_equal(got.view(np.uint64), host.view(np.uint64))
+        assert np.array_equal(anyh["prim"] != orc.NO_HIT, ref["prim"] != orc.NO_HIT)
+        hit = np.nonzero(anyh["prim"] != orc.NO_HIT)[0]
+        assert np.all(anyh["t"][hit] >= got["t"][hit])
+
+
+def test_mt_mode_rejected_where_unsupported(rt, cuda):
+    """rt_trace_count and the pool have no Moller-Trumbore instantiation: the
+    flag is refused with RT_EINVAL, not ignored."""
+    tris, _, rays = rt.gen_config1()
+    with rt.Scene(tris) as sc:
+        d_rays = cuda.from_numpy(np.ascontiguousarray(rays[:1024]).view(np.uint8)).cuda()
+        d_hits = cuda.empty(1024 * 8, dtype=cuda.uint8, device="cuda")
+        c = (C.c_uint64 * 2)()
+        st = rt.lib().rt_trace_count(sc.handle, d_rays.data_ptr(), 1024, d_hits.data_ptr(), rt.TRACE_MT, None, c)
+        assert rt.STATUS[st] == "RT_EINVAL"

@@ -259,8 +259,10 @@ def test_mt_restatement_matches_numpy(rt, orc):
 def _mt_explained(tri, ray, t_mt, t_plane, extent):
     """Why a Moller-Trumbore hit can differ from the plane test's: the ray
     grazes the plane (|n.d| < 1e-4, rejected by the reference), the hit lies on
-    an edge (a barycentric within 1e-5 of 0, or u+v of 1, in binary64), or the
-    two answers are a near-tie in t."""
+    an edge (in binary64 a barycentric within 1e-4 / |n.d| of 0, or u+v of 1:
+    both tests round the hit point at the scale of the coordinates, not of the
+    triangle, and the plane test's point moves along the ray by t's error), or
+    the two answers are a near-tie in t."""
     v0, v1, v2 = (tri[k][:3].astype(np.float64) for k in ("v0", "v1", "v2"))
     o, d = ray["org"][0].astype(np.float64), ray["dir"][0].astype(np.float64)
     n = np.cross(v1 - v0, v2 - v0)
@@ -274,7 +276,7 @@ def _mt_explained(tri, ray, t_mt, t_plane, extent):
     e1, e2, q = v1 - v0, v2 - v0, p - v0
     m = np.array([[e1 @ e1, e1 @ e2], [e1 @ e2, e2 @ e2]])
     u, v = np.linalg.solve(m, np.array([q @ e1, q @ e2]))
-    if min(abs(u), abs(v), abs(1 - u - v)) < 1e-5:
+    if min(abs(u), abs(v), abs(1 - u - v)) < 1e-4 / max(abs(n @ d), 1e-4):
         return "edge"
     if np.isfinite(t_plane) and abs(t_mt - t_plane) <= 1e-5 * max(abs(t_mt), extent):
         return "near-tie"
@@ -284,15 +286,18 @@ def _mt_explained(tri, ray, t_mt, t_plane, extent):
 def test_mt_divergence_set(rt, orc):
     """The Moller-Trumbore mode against the reference's plane test: hit ids
     agree except on grazing rays, edge hits and near-ties; matching hits agree
-    in t within 1e-5 of max(t, scene extent) (the plane test's t cancels for
-    hits near the ray origin)."""
+    in t within 1e-5 of max(t, scene extent) plus 1e-7 / |n.d| (the plane
+    test's t cancels for hits near the ray origin and near grazing).  Config 1, a soup, and the first 131,072 rays of
+    config 3 (about 1 in 12,000 of them differ there, every one at an edge)."""
     cases = []
     tris, _, rays = rt.gen_config1()
-    cases.append((tris, rays[::3], 20.0))
+    cases.append((tris, rays[::3], 20.0, False))
     soup = rt.gen_soup(22, 0, 50_000, 1.0, 0.004)
-    cases.append((soup, rt.gen_rays(22, 0, 20_000, 1.0, 1e-4, float("inf")), 1.0))
-    for tris, rays, extent in cases:
-        nodes, _, _, _ = orc.build_bvh(tris, mode=0)
+    cases.append((soup, rt.gen_rays(22, 0, 20_000, 1.0, 1e-4, float("inf")), 1.0, False))
+    soup3 = rt.gen_soup(3, 0, 4_194_304, 1.0, 0.002)
+    cases.append((soup3, rt.gen_rays(3, 0, 131_072, 1.0, 1e-4, float("inf")), 1.0, True))
+    for tris, rays, extent, sah in cases:
+        nodes = rt.build_bvh_sah(tris) if sah else orc.build_bvh(tris, mode=0)[0]
         S = orc.Scene(tris, nodes)
         plane, _ = orc.trace(S, rays, canonical=True)
         mt, _ = orc.trace(S, rays, canonical=True, mt=True)
@@ -300,7 +305,14 @@ def test_mt_divergence_set(rt, orc):
         both = same & (plane["prim"] != orc.NO_HIT)
         assert both.sum() > 0.1 * len(rays)
         dt = np.abs(plane["t"][both].astype(np.float64) - mt["t"][both])
-        assert np.all(dt <= 1e-5 * np.maximum(np.abs(mt["t"][both]), extent))
+        # the plane test's t = (D - n.o) / (n.d) carries D - n.o's absolute
+        # rounding divided by n.d, so the bound grows as the ray grazes
+        hit = tris[plane["prim"][both]]
+        v0, v1, v2 = (hit[k][:, :3].astype(np.float64) for k in ("v0", "v1", "v2"))
+        n = np.cross(v1 - v0, v2 - v0)
+        n /= np.linalg.norm(n, axis=1, keepdims=True)
+        nd = np.abs(np.sum(n * rays["dir"][both].astype(np.float64), axis=1))
+        assert np.all(dt <= 1e-5 * np.maximum(np.abs(mt["t"][both]), extent) + 1e-7 / nd)
         diff = np.nonzero(~same)[0]
         assert len(diff) <= 0.01 * len(rays)
         for i in diff:
