@@ -3,9 +3,10 @@
 Compute-sanitizer is not available, so a second library,
 librt_gb300_checked.so, checks every node, primitive, ray, material and path
 index its kernels use and records violations in a per-scene word instead of
-faulting.  A subprocess runs ray queries (both node layouts, sorted and
-any-hit, deep stacks, host buffers) and wavefront renders through it; every
-check word must stay clear and every result must equal the normal build's.
+faulting.  A subprocess runs ray queries (both node layouts, sorted, any-hit,
+Moller-Trumbore, deep stacks, host buffers) and wavefront renders (two pixel
+chunks on two streams) through it; every check word must stay clear and
+every result must equal the normal build's.
 """
 import os
 import subprocess
@@ -40,6 +41,7 @@ for w in (2, 4):
         out[f"soup{w}"] = dev(sc, rays3)
         out[f"soup{w}_sort"] = dev(sc, rays3, sort=True)
         out[f"soup{w}_any"] = dev(sc, rays3, any_hit=True)
+        out[f"soup{w}_mt"] = dev(sc, rays3, mt=True)
         out[f"soup{w}_host"] = sc.trace_host(rays3).view(np.uint64)
         checks.append(sc.device_checks())
 t1, ubo1, r1 = rt.gen_config1()
@@ -59,10 +61,11 @@ tris2, mats2 = rt.gen_spheres_scene(2, 64, 3, 0.05)
 ubo2 = rt.make_ubo((0.0, 3.0, 28.0), (0.0, 0.0, 0.0), fov=40.0, depth=8, random_state=2,
                    num_triangles=len(tris2), num_materials=len(mats2))
 with rt.Scene(tris2, materials=mats2) as sc:
-    acc = torch.empty(160 * 90 * 4, dtype=torch.float32, device="cuda")
+    # 320 x 240 x 4 samples: the frame runs as two pixel chunks on two streams
+    acc = torch.empty(320 * 240 * 4, dtype=torch.float32, device="cuda")
     for mode in (rt.SHADE_EXTENDED, rt.SHADE_REFERENCE):
-        rt.accum_clear(acc, 160, 90)
-        sc.render(ubo2, acc, 160, 90, 4, shade_mode=mode, background=(0.6, 0.7, 1.0))
+        rt.accum_clear(acc, 320, 240)
+        sc.render(ubo2, acc, 320, 240, 4, shade_mode=mode, background=(0.6, 0.7, 1.0))
         torch.cuda.synchronize()
         out[f"render{mode}"] = acc.cpu().numpy()
     checks.append(sc.device_checks())
