@@ -299,7 +299,7 @@ TraceTuning default_tuning() {
   static TraceTuning t = [] {
     TraceTuning d;
     d.variant = env_int("RT_TRACE_VARIANT", 6);
-    d.refill = env_int("RT_TRACE_REFILL", 4);
+    d.refill = env_int("RT_TRACE_REFILL", 5);
     d.grid_scale = env_int("RT_TRACE_GRID_PCT", 100);
     return d;
   }();
