@@ -604,36 +604,45 @@ cudaError_t launch_render_wave(const DeviceScene& S, const Cam& cam, uint32_t de
     for (int k = 1; k < used; ++k)
       if ((e = cudaStreamWaitEvent(sts[k], streams->fork, 0)) != cudaSuccess) return e;
   }
-  uint32_t chunk = 0;
-  for (uint32_t pix0 = 0; pix0 < total; pix0 += q_chunk, ++chunk) {
-    const uint32_t q = std::min(q_chunk, total - pix0);
-    const WaveBufs& B = Bs[chunk % (uint32_t)used];
-    const cudaStream_t cs = sts[chunk % (uint32_t)used];
-    for (uint32_t s0 = 0; s0 < spp; s0 += ns_pass) {
-      const uint32_t ns = std::min(ns_pass, spp - s0);
-      const uint32_t np = q * ns;
-      if ((e = cudaMemsetAsync(B.cnt, 0, 16 * ((size_t)depth + 1), cs)) != cudaSuccess) return e;
-      const uint32_t gb = std::min<uint32_t>(sms * 8, (q + 255) / 256);
-      k_wave_seed<<<gb, 256, 0, cs>>>(cam, rs, accum, Wd, pix0, q, ns, per_path, B.rng0, B.rays[0]);
-      for (uint32_t l = 0; l < depth; ++l) {
-        const float4* r = B.rays[l & 1u];
-        if ((e = launch_trace_raw(S, r, l == 0 ? (per_path ? np : q) : 0xFFFFFFFFu, B.hits, B.cnt + 4u * l,
-                                  trace_stats, cs)) != cudaSuccess)
-          return e;
-        const uint32_t gs = l == 0 ? std::min<uint32_t>(sms * 8, (np + 255) / 256) : sms * 8;
-        k_wave_shade<STATS><<<gs, 256, 0, cs>>>(S, l, depth, np, q, ns, per_path, mode, bg[0], bg[1], bg[2], B.state,
-                                                B.rng0, r, B.list[l & 1u], B.hits, B.rays[(l + 1u) & 1u],
-                                                B.list[(l + 1u) & 1u], B.cnt, counter + 1, stats);
+  auto chunks = [&]() -> cudaError_t {
+    cudaError_t e2;
+    uint32_t chunk = 0;
+    for (uint32_t pix0 = 0; pix0 < total; pix0 += q_chunk, ++chunk) {
+      const uint32_t q = std::min(q_chunk, total - pix0);
+      const WaveBufs& B = Bs[chunk % (uint32_t)used];
+      const cudaStream_t cs = sts[chunk % (uint32_t)used];
+      for (uint32_t s0 = 0; s0 < spp; s0 += ns_pass) {
+        const uint32_t ns = std::min(ns_pass, spp - s0);
+        const uint32_t np = q * ns;
+        if ((e2 = cudaMemsetAsync(B.cnt, 0, 16 * ((size_t)depth + 1), cs)) != cudaSuccess) return e2;
+        const uint32_t gb = std::min<uint32_t>(sms * 8, (q + 255) / 256);
+        k_wave_seed<<<gb, 256, 0, cs>>>(cam, rs, accum, Wd, pix0, q, ns, per_path, B.rng0, B.rays[0]);
+        for (uint32_t l = 0; l < depth; ++l) {
+          const float4* r = B.rays[l & 1u];
+          if ((e2 = launch_trace_raw(S, r, l == 0 ? (per_path ? np : q) : 0xFFFFFFFFu, B.hits, B.cnt + 4u * l,
+                                     trace_stats, cs)) != cudaSuccess)
+            return e2;
+          const uint32_t gs = l == 0 ? std::min<uint32_t>(sms * 8, (np + 255) / 256) : sms * 8;
+          k_wave_shade<STATS><<<gs, 256, 0, cs>>>(S, l, depth, np, q, ns, per_path, mode, bg[0], bg[1], bg[2],
+                                                  B.state, B.rng0, r, B.list[l & 1u], B.hits,
+                                                  B.rays[(l + 1u) & 1u], B.list[(l + 1u) & 1u], B.cnt,
+                                                  counter + 1, stats);
+        }
+        k_wave_accum<<<gb, 256, 0, cs>>>(accum, pix0, q, ns, B.state);
+        if ((e2 = cudaGetLastError()) != cudaSuccess) return e2;
       }
-      k_wave_accum<<<gb, 256, 0, cs>>>(accum, pix0, q, ns, B.state);
-      if ((e = cudaGetLastError()) != cudaSuccess) return e;
     }
-  }
+    return cudaSuccess;
+  };
+  e = chunks();
+  // the caller's stream waits for every extra stream, also after a failed
+  // launch, so that nothing of this call is left unordered behind it
   for (int k = 1; k < used; ++k) {
-    if ((e = cudaEventRecord(streams->join[k - 1], sts[k])) != cudaSuccess) return e;
-    if ((e = cudaStreamWaitEvent(st, streams->join[k - 1], 0)) != cudaSuccess) return e;
+    cudaError_t ej = cudaEventRecord(streams->join[k - 1], sts[k]);
+    if (ej == cudaSuccess) ej = cudaStreamWaitEvent(st, streams->join[k - 1], 0);
+    if (e == cudaSuccess) e = ej;
   }
-  return cudaGetLastError();
+  return e != cudaSuccess ? e : cudaGetLastError();
 }
 
 __global__ void k_clear(float4* accum, uint32_t total) {
