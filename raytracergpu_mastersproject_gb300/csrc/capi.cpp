@@ -611,31 +611,44 @@ rt_status rt_trace_host(rt_scene* scene, const RtRay* h_rays, uint32_t n, RtHit*
   // through copy_in's events)
   if ((e = cudaEventRecord(w->ev[6], st)) != cudaSuccess) return cuda_fail(e, "event");
   if ((e = cudaStreamWaitEvent(w->copy_in, w->ev[6], 0)) != cudaSuccess) return cuda_fail(e, "wait");
-  uint32_t size = std::min(chunk, kFirstChunk), chunks = 0;
-  for (uint32_t c = 0, off = 0, cnt = 0; off < n;
-       ++c, off += cnt, size = (uint32_t)std::min<uint64_t>((uint64_t)growth * size, chunk)) {
-    const uint32_t b = c & 1u;
-    cnt = std::min(size, n - off);
-    chunks = c + 1;
-    if (c >= 2 && (e = cudaStreamWaitEvent(w->copy_in, free_again[b], 0)) != cudaSuccess) return cuda_fail(e, "wait");
-    if ((e = cudaMemcpyAsync(drays[b], h_rays + off, (size_t)cnt * sizeof(RtRay), cudaMemcpyHostToDevice,
-                             w->copy_in)) != cudaSuccess)
-      return cuda_fail(e, "rt_trace_host: H2D");
-    if ((e = cudaEventRecord(in_done[b], w->copy_in)) != cudaSuccess) return cuda_fail(e, "event");
-    if ((e = cudaStreamWaitEvent(tst[b], in_done[b], 0)) != cudaSuccess) return cuda_fail(e, "wait");
-    uint32_t* order = nullptr;
-    if ((s = maybe_reorder(w, scene->d, drays[b], cnt, flags, tst[b], &order, b * slot)) != RT_OK) return s;
-    if ((e = cudaMemsetAsync(counters[b], 0, 2 * sizeof(uint32_t), tst[b])) != cudaSuccess) return cuda_fail(e, "memset");
-    RtHit* out = direct ? direct + off : dhits[b];
-    if ((e = launch_trace(scene->d, drays[b], cnt, out, flags, counters[b], tst[b], order)) != cudaSuccess)
-      return cuda_fail(e, "rt_trace_host: launch");
-    if ((e = cudaEventRecord(trace_done[b], tst[b])) != cudaSuccess) return cuda_fail(e, "event");
-    if (direct) continue;
-    if ((e = cudaStreamWaitEvent(w->copy_out, trace_done[b], 0)) != cudaSuccess) return cuda_fail(e, "wait");
-    if ((e = cudaMemcpyAsync(h_hits + off, dhits[b], (size_t)cnt * sizeof(RtHit), cudaMemcpyDeviceToHost,
-                             w->copy_out)) != cudaSuccess)
-      return cuda_fail(e, "rt_trace_host: D2H");
-    if ((e = cudaEventRecord(out_done[b], w->copy_out)) != cudaSuccess) return cuda_fail(e, "event");
+  uint32_t chunks = 0;
+  auto enqueue = [&]() -> rt_status {
+    uint32_t size = std::min(chunk, kFirstChunk);
+    for (uint32_t c = 0, off = 0, cnt = 0; off < n;
+         ++c, off += cnt, size = (uint32_t)std::min<uint64_t>((uint64_t)growth * size, chunk)) {
+      const uint32_t b = c & 1u;
+      cnt = std::min(size, n - off);
+      chunks = c + 1;
+      if (c >= 2 && (e = cudaStreamWaitEvent(w->copy_in, free_again[b], 0)) != cudaSuccess)
+        return cuda_fail(e, "wait");
+      if ((e = cudaMemcpyAsync(drays[b], h_rays + off, (size_t)cnt * sizeof(RtRay), cudaMemcpyHostToDevice,
+                               w->copy_in)) != cudaSuccess)
+        return cuda_fail(e, "rt_trace_host: H2D");
+      if ((e = cudaEventRecord(in_done[b], w->copy_in)) != cudaSuccess) return cuda_fail(e, "event");
+      if ((e = cudaStreamWaitEvent(tst[b], in_done[b], 0)) != cudaSuccess) return cuda_fail(e, "wait");
+      uint32_t* order = nullptr;
+      rt_status rs = maybe_reorder(w, scene->d, drays[b], cnt, flags, tst[b], &order, b * slot);
+      if (rs != RT_OK) return rs;
+      if ((e = cudaMemsetAsync(counters[b], 0, 2 * sizeof(uint32_t), tst[b])) != cudaSuccess)
+        return cuda_fail(e, "memset");
+      RtHit* out = direct ? direct + off : dhits[b];
+      if ((e = launch_trace(scene->d, drays[b], cnt, out, flags, counters[b], tst[b], order)) != cudaSuccess)
+        return cuda_fail(e, "rt_trace_host: launch");
+      if ((e = cudaEventRecord(trace_done[b], tst[b])) != cudaSuccess) return cuda_fail(e, "event");
+      if (direct) continue;
+      if ((e = cudaStreamWaitEvent(w->copy_out, trace_done[b], 0)) != cudaSuccess) return cuda_fail(e, "wait");
+      if ((e = cudaMemcpyAsync(h_hits + off, dhits[b], (size_t)cnt * sizeof(RtHit), cudaMemcpyDeviceToHost,
+                               w->copy_out)) != cudaSuccess)
+        return cuda_fail(e, "rt_trace_host: D2H");
+      if ((e = cudaEventRecord(out_done[b], w->copy_out)) != cudaSuccess) return cuda_fail(e, "event");
+    }
+    return RT_OK;
+  };
+  if ((s = enqueue()) != RT_OK) {
+    // nothing this call enqueued may still touch h_rays or h_hits after it
+    // returns: wait for the helper streams and the caller's stream
+    for (cudaStream_t h : {w->copy_in, w->trace2, w->copy_out, st}) cudaStreamSynchronize(h);
+    return s;
   }
   if (direct) {
     // the caller's stream continues after trace2's last chunk; its own chunks
