@@ -282,9 +282,7 @@ rt_status rt_build_bvh_sah(const RtTriangle64* triangles, uint32_t num_triangles
     set_error("rt_build_bvh_sah: " + msg);
     return RT_EINVAL;
   }
-  std::vector<RtBVHNode40> nodes;
-  build_sah(wt.data(), num_triangles, ws.data(), num_spheres, nodes);
-  if (!nodes.empty()) std::memcpy(out_nodes, nodes.data(), nodes.size() * sizeof(RtBVHNode40));
+  build_sah(wt.data(), num_triangles, ws.data(), num_spheres, out_nodes);
   return RT_OK;
 }
 
@@ -343,18 +341,19 @@ rt_status rt_scene_create_ex(const RtSceneDesc* desc, rt_scene** out_scene) {
     return RT_EINVAL;
   }
   // the traversal tree: SAH for library-built sorted-mode scenes, else S1
-  std::vector<RtBVHNode40> sah;
   const bool use_sah = !desc->nodes && !(desc->build_flags & (RT_BUILD_ON_DEVICE | RT_BUILD_TRAVERSE_S1)) &&
                        desc->bvh_mode == RT_BVH_SORTED && N > 1;
-  if (use_sah) build_sah(wt.data(), nt, ws.data(), ns, sah);
-  const std::vector<RtBVHNode40>& trav = use_sah ? sah : sc->nodes40;
-  if (!convert_bvh(trav.data(), (uint32_t)trav.size(), wt.data(), nt, ws.data(), ns, desc->materials, nm,
+  std::unique_ptr<RtBVHNode40[]> sah(use_sah ? new RtBVHNode40[2 * N - 1] : nullptr);
+  if (use_sah) build_sah(wt.data(), nt, ws.data(), ns, sah.get());
+  const RtBVHNode40* trav = use_sah ? sah.get() : sc->nodes40.data();
+  const uint32_t trav_n = use_sah ? (uint32_t)(2 * N - 1) : (uint32_t)sc->nodes40.size();
+  if (!convert_bvh(trav, trav_n, wt.data(), nt, ws.data(), ns, desc->materials, nm,
                    desc->leaf_size, width, hb, msg)) {
     set_error("rt_scene_create_ex: " + msg);
     return RT_EINVAL;
   }
   if (hb.width == 4 && hb.stack_need > 192u) {  // too deep for the wide stack: binary form
-    if (!convert_bvh(trav.data(), (uint32_t)trav.size(), wt.data(), nt, ws.data(), ns, desc->materials,
+    if (!convert_bvh(trav, trav_n, wt.data(), nt, ws.data(), ns, desc->materials,
                      nm, desc->leaf_size, 2, hb, msg)) {
       set_error("rt_scene_create_ex: " + msg);
       return RT_EINVAL;

@@ -21,6 +21,7 @@
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
+#include <memory>
 #include <thread>
 
 #include "rt_internal.h"
@@ -377,8 +378,10 @@ struct SahBin {
 
 struct SahBuild {
   uint32_t nt = 0;
-  std::vector<SahRec> rec, tmp;
-  std::vector<RtBVHNode40>* out = nullptr;
+  // uninitialised (no zero fill): every record and node is written before it
+  // is read, by the threads that build, so the first-touch faults spread too
+  std::unique_ptr<SahRec[]> rec, tmp;
+  RtBVHNode40* out = nullptr;
   std::atomic<uint32_t> next{1};
 
   static void set_box(RtBVHNode40& nd, const SahBox& b) {
@@ -387,7 +390,7 @@ struct SahBuild {
     nd.minZ = b.lo[2]; nd.maxZ = b.hi[2];
   }
   void leaf(uint32_t node, const SahRec& r) {
-    RtBVHNode40& nd = (*out)[node];
+    RtBVHNode40& nd = out[node];
     SahBox b;
     b.grow(r.lo, r.hi);
     set_box(nd, b);
@@ -423,8 +426,8 @@ struct SahBuild {
   template <class P>
   size_t partition(size_t b, size_t e, bool par, P left) {
     if (!par) {
-      SahRec* m = std::partition(rec.data() + b, rec.data() + e, left);
-      return (size_t)(m - rec.data());
+      SahRec* m = std::partition(rec.get() + b, rec.get() + e, left);
+      return (size_t)(m - rec.get());
     }
     const unsigned T = host_threads();
     const size_t n = e - b, per = (n + T - 1) / T;
@@ -463,7 +466,7 @@ struct SahBuild {
   size_t split(uint32_t node, size_t b, size_t e, bool par, int depth) {
     SahBox box, cb;
     bounds(b, e, par, box, cb);
-    set_box((*out)[node], box);
+    set_box(out[node], box);
     const size_t n = e - b;
     int wide = 0;
     for (int k = 1; k < 3; ++k)
@@ -471,11 +474,11 @@ struct SahBuild {
     auto by_axis = [wide](const SahRec& p, const SahRec& q) { return p.c[wide] < q.c[wide]; };
     if (depth >= kSahDepth) {
       const size_t mid = b + n / 2;
-      std::nth_element(rec.begin() + (ptrdiff_t)b, rec.begin() + (ptrdiff_t)mid, rec.begin() + (ptrdiff_t)e, by_axis);
+      std::nth_element(rec.get() + (ptrdiff_t)b, rec.get() + (ptrdiff_t)mid, rec.get() + (ptrdiff_t)e, by_axis);
       return mid;
     }
     if (n <= kSahSweep) {
-      std::sort(rec.begin() + (ptrdiff_t)b, rec.begin() + (ptrdiff_t)e, by_axis);
+      std::sort(rec.get() + (ptrdiff_t)b, rec.get() + (ptrdiff_t)e, by_axis);
       double right[kSahSweep];
       SahBox acc;
       for (size_t i = n - 1; i > 0; --i) {
@@ -568,10 +571,10 @@ struct SahBuild {
     const uint32_t c = next.fetch_add(2);
     l = c;
     r = c + 1;
-    (*out)[node].left = l;
-    (*out)[node].right = r;
-    (*out)[node].primitiveIndex = 0;
-    (*out)[node].primitiveType = 0;
+    out[node].left = l;
+    out[node].right = r;
+    out[node].primitiveIndex = 0;
+    out[node].primitiveType = 0;
   }
   void build_serial(uint32_t node, size_t b, size_t e, int depth) {
     if (e - b == 1) {
@@ -588,16 +591,14 @@ struct SahBuild {
 
 }  // namespace
 
-void build_sah(const RtTriangle64* tris, uint32_t nt, const RtSphere32* sph, uint32_t ns,
-               std::vector<RtBVHNode40>& out) {
+void build_sah(const RtTriangle64* tris, uint32_t nt, const RtSphere32* sph, uint32_t ns, RtBVHNode40* out) {
   const size_t N = (size_t)nt + ns;
-  out.assign(N ? 2 * N - 1 : 0, RtBVHNode40{});
   if (N == 0) return;
   SahBuild B;
   B.nt = nt;
-  B.out = &out;
-  B.rec.resize(N);
-  if (N > kSahTask) B.tmp.resize(N);
+  B.out = out;
+  B.rec.reset(new SahRec[N]);
+  if (N > kSahTask) B.tmp.reset(new SahRec[N]);
   parallel_for(N, [&](size_t b, size_t e, unsigned) {
     for (size_t i = b; i < e; ++i) {
       SahRec& r = B.rec[i];
@@ -636,24 +637,34 @@ void build_sah(const RtTriangle64* tris, uint32_t nt, const RtSphere32* sph, uin
     int depth;
   };
   std::vector<Range> open{{0u, 0, N, 0}}, tasks;
+  const unsigned T = std::max(1u, host_threads());
   while (!open.empty()) {
-    std::vector<Range> nxt;
-    for (const Range& r : open) {
-      if (r.e - r.b <= kSahTask) {
-        tasks.push_back(r);
-        continue;
-      }
-      const size_t mid = B.split(r.node, r.b, r.e, true, r.depth);
+    std::vector<Range> big;
+    for (const Range& r : open) (r.e - r.b <= kSahTask ? tasks : big).push_back(r);
+    std::vector<Range> nxt(2 * big.size());
+    auto one = [&](size_t i, bool par) {
+      const Range& r = big[i];
+      const size_t mid = B.split(r.node, r.b, r.e, par, r.depth);
       uint32_t l, rr;
       B.children(r.node, l, rr);
-      nxt.push_back({l, r.b, mid, r.depth + 1});
-      nxt.push_back({rr, mid, r.e, r.depth + 1});
+      nxt[2 * i] = {l, r.b, mid, r.depth + 1};
+      nxt[2 * i + 1] = {rr, mid, r.e, r.depth + 1};
+    };
+    if (big.size() >= T) {  // a range per thread, each split serially
+      std::atomic<size_t> ri{0};
+      std::vector<std::thread> th;
+      for (unsigned t = 0; t < T; ++t)
+        th.emplace_back([&] {
+          for (size_t k; (k = ri.fetch_add(1)) < big.size();) one(k, false);
+        });
+      for (auto& x : th) x.join();
+    } else {  // few ranges: each split's passes spread over the threads
+      for (size_t i = 0; i < big.size(); ++i) one(i, true);
     }
     open.swap(nxt);
   }
   std::sort(tasks.begin(), tasks.end(), [](const Range& a, const Range& b) { return a.e - a.b > b.e - b.b; });
   std::atomic<size_t> ti{0};
-  const unsigned T = std::max(1u, host_threads());
   std::vector<std::thread> th;
   for (unsigned t = 0; t < T; ++t)
     th.emplace_back([&] {

@@ -511,19 +511,21 @@ rt_status rt_pool_add_scene(rt_pool* P, const RtSceneDesc* desc, uint32_t* out_i
   const bool use_sah = !desc->nodes && !(desc->build_flags & (RT_BUILD_ON_DEVICE | RT_BUILD_TRAVERSE_S1)) &&
                        desc->bvh_mode == RT_BVH_SORTED && nt > 1;
   std::vector<RtBVHNode40> nodes;
+  std::unique_ptr<RtBVHNode40[]> sah(use_sah ? new RtBVHNode40[2 * (size_t)nt - 1] : nullptr);
   if (desc->nodes) {
     nodes.assign(desc->nodes, desc->nodes + (nt ? 2 * (size_t)nt - 1 : 0));
   } else if ((desc->build_flags & RT_BUILD_ON_DEVICE) && nt) {
     rt_status bs = device_build_to_host(wt.data(), nt, nullptr, 0, desc->bvh_mode, nodes);
     if (bs != RT_OK) return bs;
   } else if (use_sah) {
-    build_sah(wt.data(), nt, nullptr, 0, nodes);
+    build_sah(wt.data(), nt, nullptr, 0, sah.get());
   } else {
     build_bvh(wt.data(), nt, nullptr, 0, desc->bvh_mode, nodes);
   }
+  const RtBVHNode40* trav = use_sah ? sah.get() : nodes.data();
+  const uint32_t trav_n = use_sah ? (uint32_t)(2 * (size_t)nt - 1) : (uint32_t)nodes.size();
   HostDeviceBVH hb;
-  if (!convert_bvh(nodes.data(), (uint32_t)nodes.size(), wt.data(), nt, nullptr, 0, nullptr, 0, desc->leaf_size, 4, hb,
-                   msg)) {
+  if (!convert_bvh(trav, trav_n, wt.data(), nt, nullptr, 0, nullptr, 0, desc->leaf_size, 4, hb, msg)) {
     set_error("rt_pool_add_scene: " + msg);
     return RT_EINVAL;
   }

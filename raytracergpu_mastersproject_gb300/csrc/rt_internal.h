@@ -133,8 +133,8 @@ bool convert_bvh(const RtBVHNode40* nodes, uint32_t nn, const RtTriangle64* tris
                  uint32_t leaf_size, uint32_t width, HostDeviceBVH& out, std::string& msg);
 // Binned-SAH traversal tree over the same primitives (triangles, then
 // spheres) in the node form convert_bvh reads; not the reference layout.
-void build_sah(const RtTriangle64* tris, uint32_t nt, const RtSphere32* sph, uint32_t ns,
-               std::vector<RtBVHNode40>& out);
+// Writes 2 * (nt + ns) - 1 nodes to out.
+void build_sah(const RtTriangle64* tris, uint32_t nt, const RtSphere32* sph, uint32_t ns, RtBVHNode40* out);
 // Camera of raytraceBVH.comp:50-81: out = camPos, pixel00, pixelDeltaU, pixelDeltaV.
 void camera_setup(const RtRaytraceUBO& ubo, uint32_t width, uint32_t height, float out[12]);
 
