@@ -2,8 +2,9 @@
 
 The reference ships no test vectors and cannot run here, so these fixtures
 freeze the oracle's own outputs (RNG streams, sin/cos, BVH node arrays,
-closest/any hits, a small path-traced accumulator) on small inputs that are
-stored alongside, so the checks do not depend on the generators' libm.
+closest/any hits, the Moller-Trumbore mode's hits, a small path-traced
+accumulator) on small inputs that are stored alongside, so the checks do not
+depend on the generators' libm.
 
     python tests/golden/make_golden.py
 """
@@ -78,7 +79,16 @@ def main():
     sh, _ = orc.trace(orc.Scene(soup, sn), srays)
     np.savez_compressed(HERE / "soup_small.npz", tris=soup.view(np.uint8), rays=srays.view(np.uint8),
                         nodes=sn.view(np.uint8), hits=sh.view(np.uint8))
+    mt_fixture()
     print("fixtures written to", HERE)
+
+
+def mt_fixture():
+    """The Moller-Trumbore mode's closest hits on the soup_small inputs."""
+    g = np.load(HERE / "soup_small.npz")
+    soup, srays, sn = g["tris"].view(orc.TRI), g["rays"].view(orc.RAY), g["nodes"].view(orc.NODE)
+    mh, _ = orc.trace(orc.Scene(soup, sn), srays, mt=True)
+    np.savez_compressed(HERE / "soup_small_mt.npz", hits=mh.view(np.uint8))
 
 
 if __name__ == "__main__":

@@ -264,7 +264,14 @@ def test_golden_fixtures_on_gpu(rt, orc, cuda):
     st, sr = s["tris"].view(rt.TRIANGLE_DTYPE), s["rays"].view(rt.RAY_DTYPE)
     with rt.Scene(st) as sc:
         got = dev_trace(rt, cuda, sc, sr)
+        d_rays = cuda.from_numpy(np.ascontiguousarray(sr).view(np.uint8)).cuda()
+        d_hits = cuda.empty(len(sr) * 8, dtype=cuda.uint8, device="cuda")
+        sc.trace(d_rays, d_hits, mt=True)
+        cuda.cuda.synchronize()
+        got_mt = d_hits.cpu().numpy().view(rt.HIT_DTYPE).copy()
     assert_parity(orc, st, sr, s["hits"].view(rt.HIT_DTYPE), got)
+    m = np.load(Path(__file__).resolve().parent / "golden" / "soup_small_mt.npz")
+    assert_mt_parity(orc, m["hits"].view(rt.HIT_DTYPE), got_mt)
 
 
 @pytest.mark.parametrize("width", [2, 4])

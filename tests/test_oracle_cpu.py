@@ -162,6 +162,15 @@ def test_golden_soup(orc):
     assert np.array_equal(hits.view(np.uint8), g["hits"])
 
 
+def test_golden_soup_moller_trumbore(orc):
+    g = np.load(GOLDEN / "soup_small.npz")
+    m = np.load(GOLDEN / "soup_small_mt.npz")
+    tris, rays, nodes = g["tris"].view(orc.TRI), g["rays"].view(orc.RAY), g["nodes"].view(orc.NODE)
+    hits, _ = orc.trace(orc.Scene(tris, nodes), rays, mt=True)
+    assert np.array_equal(hits.view(np.uint8), m["hits"])
+    assert (hits["prim"] != orc.NO_HIT).sum() > 100
+
+
 # --------------------------------------------------------- traversal ------
 def test_reference_and_canonical_orders_agree(rt, orc):
     tris, ubo, rays = rt.gen_config1()
