@@ -14,11 +14,13 @@ roofline: algorithmic bytes per ray (32 ray + 8 hit + 32 per node box tested
          + 48 per triangle tested, counts of the canonical traversal) times
          rays per launch over the kernel's event-timed launch duration,
          against the measured HBM copy bandwidth
-cpu_baseline: the CPU oracle's restatement of the reference traversal
-         (raytraceBVH.comp:195-265, push-left/go-right, no culling) on a
-         bounded sample of the same rays, all host threads
+cpu_baseline: the reference's traversal (raytraceBVH.comp:195-265,
+         push-left/go-right, no culling) on the host cores -- its own GLSL
+         compiled as C++ (oracle/ref_glsl.py) where available, else the
+         oracle's restatement -- on a bounded sample of the same rays, all
+         host threads
 
---impl reference runs that CPU restatement alone as the reference arm.
+--impl reference runs that CPU traversal alone as the reference arm.
 """
 from __future__ import annotations
 
@@ -191,20 +193,23 @@ def cpu_leg(tris, nodes, rays, sample: int, trav_nodes=None) -> tuple[dict, dict
     (`trav_nodes`, default the S1 tree)."""
     from oracle import oracle as orc
 
-    orc.build()
+    trace, kind, what = reference_tracer()
     S = orc.Scene(tris, nodes)
     cores = os.cpu_count() or 1
     sub = np.ascontiguousarray(rays[:sample])
 
     def rate(scene, r, canonical, threads):
         t0 = time.perf_counter()
-        orc.trace(scene, r, canonical=canonical, nthreads=threads)
+        if canonical:
+            orc.trace(scene, r, canonical=True, nthreads=threads)
+        else:
+            trace(scene, r, threads)
         return len(r) / (time.perf_counter() - t0) / 1e9
 
     quarter = np.ascontiguousarray(rays[:max(1, sample // 4)])
     runs = [rate(S, quarter, False, cores) for _ in range(5)]
     t0 = time.perf_counter()
-    ref_hits, st = orc.trace(S, sub, canonical=False, nthreads=cores)
+    ref_hits = trace(S, sub, cores)
     dt = time.perf_counter() - t0
     cnt = sub
     St = S if trav_nodes is None else orc.Scene(tris, trav_nodes)
@@ -217,9 +222,9 @@ def cpu_leg(tris, nodes, rays, sample: int, trav_nodes=None) -> tuple[dict, dict
               "canonical": rate(St, one_can, True, 1), "canonical_rays": len(one_can), "unit": UNIT}
     counts = {"node_boxes_per_ray": float(cst[0]) / len(cnt), "tri_tests_per_ray": float(cst[1]) / len(cnt),
               "sample": len(cnt)}
-    base = {"value": float(np.median(runs)), "unit": UNIT, "cores": cores, "kind": "port",
-            "sample": f"median of 5 runs over the first {len(quarter)} rays of the config-3 batch, oracle "
-                      f"restatement of hitBVH (reference order, no culling, sorted-leaf BVH), {cores} threads",
+    base = {"value": float(np.median(runs)), "unit": UNIT, "cores": cores, "kind": kind,
+            "sample": f"median of 5 runs over the first {len(quarter)} rays of the config-3 batch, {what} "
+                      f"(reference order, no culling, sorted-leaf S1 tree), {cores} threads",
             "runs": runs,
             "full_sample": {"rays": len(sub), "value": len(sub) / dt / 1e9, "seconds": dt},
             "single_thread": single,
@@ -433,28 +438,59 @@ def run_served(torch, rt, n_requests: int, rates: list[float]) -> dict:
             "sequential": "same server, one query per launch, one launch at a time"}
 
 
+def reference_tracer():
+    """-> (trace(scene, rays, nthreads) -> hits, kind, description) of the
+    reference's traversal on the host: its own hitBVH (raytraceBVH.comp:195-265)
+    compiled from the shader source when oracle/_ref has it, else the oracle's
+    line-by-line restatement."""
+    from oracle import oracle as orc
+
+    orc.build()
+    try:
+        from oracle import ref
+
+        if ref.available():
+            return (lambda S, r, nth: ref.trace(S, r, nthreads=nth), "reference",
+                    "the reference's own hitBVH (raytraceBVH.comp:195-265) compiled from its GLSL source as host "
+                    "C++ (oracle/ref_glsl.py)")
+    except (ImportError, OSError, RuntimeError):
+        pass
+    return (lambda S, r, nth: orc.trace(S, r, nthreads=nth)[0], "port",
+            "oracle restatement of hitBVH (raytraceBVH.comp:195-265)")
+
+
 def run_reference(args):
-    """Reference arm: the CPU restatement of the reference traversal, timed."""
+    """Reference arm: the reference's traversal on the host cores, timed on
+    bounded samples.  Inputs come from the oracle's copy of the generators and
+    the BVH from the oracle's transcription of the six S1 passes, so this arm
+    loads nothing of the product library."""
     ws, rank, _ = dist_env()
     if rank != 0:
         return
-    import raytracergpu_mastersproject_gb300 as rt
     from oracle import oracle as orc
 
-    tris, rays = workload(args.tris, args.rays)
-    nodes = rt.build_bvh(tris)
-    orc.build()
+    trace, kind, what = reference_tracer()
+    tris = orc.gen_soup(SEED, 0, args.tris, 1.0, 0.002)
+    nodes = orc.build_bvh(tris, mode=0)[0]
     S = orc.Scene(tris, nodes)
     cores = os.cpu_count() or 1
     per = max(1024, min(args.cpu_sample, 65_536))
+    total = per * (args.warmup + args.steps)
+    rays = orc.gen_rays(SEED, 0, min(total, args.rays), 1.0, 1e-4, float("inf"))
     off = 0
+
+    def step():
+        nonlocal off
+        if off + per > len(rays):
+            off = 0
+        trace(S, rays[off:off + per], cores)
+        off += per
+
     for _ in range(args.warmup):
-        orc.trace(S, rays[off:off + per], nthreads=cores)
-        off = (off + per) % (len(rays) - per)
+        step()
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        orc.trace(S, rays[off:off + per], nthreads=cores)
-        off = (off + per) % (len(rays) - per)
+        step()
     dt = time.perf_counter() - t0
     v = per * args.steps / dt / 1e9
     line = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
@@ -464,10 +500,9 @@ def run_reference(args):
             "config": {"workload": f"config 3: {args.tris}-triangle soup, incoherent rays, closest-hit; "
                                    f"each step traces a bounded sample of {per} rays on the host cores",
                        "triangles": args.tris, "rays_per_step": per},
-            "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
-                             "sample": f"{per} rays per step, oracle restatement of hitBVH (reference order, "
-                                       f"no culling, sorted-leaf BVH); the reference itself is Vulkan/GLSL and "
-                                       f"cannot run here"},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": kind,
+                             "sample": f"{per} consecutive rays of the config-3 batch per step, {what}, over the "
+                                       f"sorted-leaf S1 tree, {cores} threads"},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 

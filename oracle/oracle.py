@@ -2,8 +2,9 @@
 
 TEST INFRASTRUCTURE ONLY: tests/, __graft_entry__.smoke() and bench.py's CPU
 baseline load this as the checker.  The product library never does.
-Parity unpinned: the reference has no tests, fixtures or golden vectors and
-cannot run here (Vulkan/GLSL); the oracle is a line-by-line restatement.
+The reference has no tests, fixtures or golden vectors and its Vulkan/GLSL
+path cannot run here; the oracle is pinned to the reference's own shaders
+compiled for the host (oracle/ref_glsl.py, tests/test_ref_pin_cpu.py).
 """
 from __future__ import annotations
 
@@ -39,8 +40,8 @@ _lib = None
 
 
 def build() -> Path:
-    src = HERE / "rt_oracle.c"
-    if not LIB.exists() or LIB.stat().st_mtime < src.stat().st_mtime:
+    newest = max((HERE / f).stat().st_mtime for f in ("rt_oracle.c", "rt_sincos.h", "build.sh"))
+    if not LIB.exists() or LIB.stat().st_mtime < newest:
         subprocess.run(["sh", str(HERE / "build.sh")], check=True, capture_output=True)
     return LIB
 
@@ -69,6 +70,8 @@ def lib() -> C.CDLL:
             "orc_triangle_test": (C.c_int, [P, P, F, C.POINTER(F)]),
             "orc_triangle_t64": (D, [P, P, C.POINTER(C.c_int)]),
             "orc_all_hits": (U, [C.POINTER(OScene), P, P, P, U]),
+            "orc_gen_soup": (None, [U64, U64, U64, U, F, F, U, P]),
+            "orc_gen_rays": (None, [U64, U64, U64, U, F, F, F, P]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(L, name)
@@ -170,6 +173,22 @@ def random_unit_vectors(state: int, n: int) -> np.ndarray:
     out = np.zeros(3 * n, np.float32)
     lib().orc_random_unit_vectors(state, n, _p(out))
     return out.reshape(n, 3)
+
+
+def gen_soup(seed: int, stream: int, n: int, side: float = 1.0, sigma: float = 0.002, material: int = 0,
+             first: int = 0) -> np.ndarray:
+    """Triangles first..first+n-1 of the library's seeded soup generator."""
+    out = np.zeros(n, TRI)
+    lib().orc_gen_soup(seed, stream, first, n, side, sigma, material, _p(out))
+    return out
+
+
+def gen_rays(seed: int, stream: int, n: int, side: float = 1.0, tmin: float = 1e-4, tmax: float = float("inf"),
+             first: int = 0) -> np.ndarray:
+    """Rays first..first+n-1 of the library's seeded ray generator."""
+    out = np.zeros(n, RAY)
+    lib().orc_gen_rays(seed, stream, first, n, side, tmin, tmax, _p(out))
+    return out
 
 
 def karras(codes) -> tuple[np.ndarray, np.ndarray]:

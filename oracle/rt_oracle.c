@@ -17,11 +17,13 @@
  *   ConstructAABBsOfInternalNodes.comp:27-64  the six BVH-build passes
  *   shaders/fragment/SingleTriangleFullScreen.frag:13-18   resolve
  *
- * Parity unpinned: the reference ships no tests, fixtures or golden vectors,
- * and it cannot run here (GLSL compute shaders behind Vulkan, no graphics
- * stack).  This file is pinned only by being a line-by-line restatement, by
- * a published worked example (Karras 2012, Fig. 3) for the tree builder, and
- * by its own committed fixtures.
+ * Pinned to the reference itself: the reference ships no tests, fixtures or
+ * golden vectors, and its Vulkan/GLSL path cannot run here, but its compute
+ * shaders compile as host C++ (oracle/ref_glsl.py), and
+ * tests/test_ref_pin_cpu.py requires this file to agree with that code bit
+ * for bit: RNG, camera, the six build passes, hitBVH and whole path-traced
+ * frames.  Also checked against a published worked example (Karras 2012,
+ * Fig. 3) and its own committed fixtures.
  *
  * Arithmetic contract (shared with the CUDA kernels; built with
  * -ffp-contract=off, no fast-math): every + - * / sqrt is one IEEE-754
@@ -112,43 +114,8 @@ static inline uint32_t f2u_sat(float f) {
 }
 
 /* ---------------------------------------------------------- sin / cos -- */
-/* Cody-Waite reduction by pi/2 in three binary32 parts, then Taylor
- * polynomials (degree 9 / 10) on [-pi/4, pi/4].  Coefficients are the
- * binary32 roundings of +-1/n!.  Identical operation order in the device code. */
-static const float RT_2_OVER_PI = 0x1.45f306p-1f;
-static const float RT_PIO2_1 = 0x1.92p+0f;
-static const float RT_PIO2_2 = 0x1.fb6p-12f;
-static const float RT_PIO2_3 = -0x1.777a5cp-25f;
-static const float RT_S1 = -0x1.555556p-3f, RT_S2 = 0x1.111112p-7f, RT_S3 = -0x1.a01a02p-13f,
-                   RT_S4 = 0x1.71de3ap-19f;
-static const float RT_C1 = -0x1p-1f, RT_C2 = 0x1.555556p-5f, RT_C3 = -0x1.6c16c2p-10f,
-                   RT_C4 = 0x1.a01a02p-16f, RT_C5 = -0x1.27e4fcp-22f;
+#include "rt_sincos.h"
 
-static void rt_sincos(float x, float* s_out, float* c_out) {
-  float kf = rintf(x * RT_2_OVER_PI);
-  int k = (int)kf;
-  float r = x - kf * RT_PIO2_1;
-  r = r - kf * RT_PIO2_2;
-  r = r - kf * RT_PIO2_3;
-  float r2 = r * r;
-  float ps = RT_S4;
-  ps = ps * r2 + RT_S3;
-  ps = ps * r2 + RT_S2;
-  ps = ps * r2 + RT_S1;
-  float s = r + r * (r2 * ps);
-  float pc = RT_C5;
-  pc = pc * r2 + RT_C4;
-  pc = pc * r2 + RT_C3;
-  pc = pc * r2 + RT_C2;
-  pc = pc * r2 + RT_C1;
-  float c = 1.0f + r2 * pc;
-  switch (k & 3) {
-    case 0: *s_out = s; *c_out = c; break;
-    case 1: *s_out = c; *c_out = -s; break;
-    case 2: *s_out = -s; *c_out = -c; break;
-    default: *s_out = -c; *c_out = s; break;
-  }
-}
 float orc_sin(float x) { float s, c; rt_sincos(x, &s, &c); return s; }
 float orc_cos(float x) { float s, c; rt_sincos(x, &s, &c); return c; }
 
@@ -992,6 +959,65 @@ int orc_build_bvh(const OTri* tris_in, uint32_t nt, const OSph* sph_in, uint32_t
   }
   free(tris); free(sph); free(mp); free(tmp); free(codes); free(parent); free(visits); free(cen);
   return 0;
+}
+
+/* ------------------------------------------------------ workload inputs -- */
+/* The seeded synthetic inputs of the benchmark (config 3 and its shapes),
+ * restated from the library's generators so that the CPU reference arm
+ * needs nothing of the product: splitmix64 keyed by (seed, stream), uniforms
+ * of 53 bits, Box-Muller in binary64, rounded to binary32 per coordinate. */
+static inline uint64_t sm64(uint64_t x) {
+  x += 0x9E3779B97F4A7C15ull;
+  x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ull;
+  x = (x ^ (x >> 27)) * 0x94D049BB133111EBull;
+  return x ^ (x >> 31);
+}
+static inline uint64_t stream_key(uint64_t seed, uint64_t stream) {
+  return sm64(sm64(seed) ^ (stream * 0xD1B54A32D192ED03ull));
+}
+static inline double u01(uint64_t key, uint64_t i) { return (double)(sm64(key + i) >> 11) * 0x1p-53; }
+static inline double gauss(uint64_t key, uint64_t i) {
+  const double u1 = u01(key, 2 * i), u2 = u01(key, 2 * i + 1);
+  return sqrt(-2.0 * log(1.0 - u1)) * cos(6.283185307179586 * u2);
+}
+
+/* Triangles first..first+n-1 of the soup (seed, stream): centroid uniform in
+ * [0, side)^3, each vertex = centroid + sigma * N(0,1) per axis. */
+void orc_gen_soup(uint64_t seed, uint64_t stream, uint64_t first, uint32_t n, float side, float sigma,
+                  uint32_t material, OTri* out) {
+  const uint64_t kc = stream_key(seed, 4 * stream + 0), kv = stream_key(seed, 4 * stream + 1);
+  for (uint32_t j = 0; j < n; ++j) {
+    const uint64_t i = first + j;
+    double c[3];
+    OTri* t = &out[j];
+    memset(t, 0, sizeof(*t));
+    for (int k = 0; k < 3; ++k) c[k] = u01(kc, 3 * i + k) * (double)side;
+    float* vs[3] = {t->v0, t->v1, t->v2};
+    for (int m = 0; m < 3; ++m)
+      for (int k = 0; k < 3; ++k) vs[m][k] = (float)(c[k] + (double)sigma * gauss(kv, 9 * i + 3 * m + k));
+    t->mat = material;
+  }
+}
+
+/* Rays first..first+n-1 of (seed, stream): origin uniform in [0, side)^3,
+ * direction a normalised Gaussian triple (uniform on the sphere). */
+void orc_gen_rays(uint64_t seed, uint64_t stream, uint64_t first, uint32_t n, float side, float tmin, float tmax,
+                  ORay* out) {
+  const uint64_t ko = stream_key(seed, 4 * stream + 2), kd = stream_key(seed, 4 * stream + 3);
+  for (uint32_t j = 0; j < n; ++j) {
+    const uint64_t i = first + j;
+    ORay* r = &out[j];
+    double g[3];
+    for (int k = 0; k < 3; ++k) {
+      r->o[k] = (float)(u01(ko, 3 * i + k) * (double)side);
+      g[k] = gauss(kd, 3 * i + k);
+    }
+    double l = sqrt(g[0] * g[0] + g[1] * g[1] + g[2] * g[2]);
+    if (l == 0.0) { g[0] = 1.0; l = 1.0; }
+    for (int k = 0; k < 3; ++k) r->d[k] = (float)(g[k] / l);
+    r->tmin = tmin;
+    r->tmax = tmax;
+  }
 }
 
 uint32_t orc_abi(void) { return 1u; }

@@ -342,3 +342,20 @@ def test_resolve_formula(orc):
     expect = np.clip(np.sqrt(np.maximum(acc.reshape(2, 4)[:, :3] / np.float32(4), 0)), 0, 1)
     assert np.allclose(out.reshape(2, 4)[:, :3], expect, atol=0)
     assert np.all(out.reshape(2, 4)[:, 3] == 1.0)
+
+
+# ------------------------------------------------------ workload inputs ---
+@pytest.mark.parametrize("seed,stream,n,side,sigma", [(3, 0, 50_000, 1.0, 0.002), (4, 17, 3_000, 0.3, 0.002),
+                                                      (11, 0, 1_000, 1.0, 0.004)])
+def test_workload_generators_match_library(rt, orc, seed, stream, n, side, sigma):
+    """The oracle's copy of the seeded generators (the CPU reference arm's
+    inputs) gives the library's triangles and rays byte for byte, also from
+    an offset into the sequence."""
+    a = rt.gen_soup(seed, stream, n, side, sigma)
+    assert np.array_equal(a.view(np.uint8), orc.gen_soup(seed, stream, n, side, sigma).view(np.uint8))
+    tail = orc.gen_soup(seed, stream, 100, side, sigma, first=n - 100)
+    assert np.array_equal(a[-100:].view(np.uint8), tail.view(np.uint8))
+    r = rt.gen_rays(seed, stream, n, side, 1e-4, float("inf"))
+    assert np.array_equal(r.view(np.uint8), orc.gen_rays(seed, stream, n, side, 1e-4, float("inf")).view(np.uint8))
+    rtail = orc.gen_rays(seed, stream, 64, side, 1e-4, float("inf"), first=n - 64)
+    assert np.array_equal(r[-64:].view(np.uint8), rtail.view(np.uint8))
