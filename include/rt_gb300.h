@@ -280,13 +280,16 @@ rt_status rt_trace_count(rt_scene* scene, const RtRay* d_rays, uint32_t n, RtHit
  * the caller's, as for rt_trace, and the results are identical.
  *
  * Its scratch is a file-scope device array of RT_NOALLOC_SCRATCH_BYTES that
- * every GPU which loads the library holds until the process exits.  The
- * first call on a device, with that device current, looks up the array's
- * device address (cudaGetSymbolAddress); make that first call before any
- * stream capture.  All calls share the one array and it keeps the last
- * call's contents (each call zeroes what must start at zero): calls that
- * overlap on the GPU -- on different streams or from different host
- * threads -- race and must be serialised by the caller.
+ * every GPU which loads the library holds until the process exits; the
+ * kernel uses its first word, the ray-queue counter.  The first call on a
+ * device, with that device current, looks up the array's device address
+ * (cudaGetSymbolAddress) and keeps it for the process; make that first call
+ * before any stream capture, and do not call across a cudaDeviceReset (the
+ * kept address would be stale; rt_trace's per-stream workspaces have the same
+ * rule).  All calls share the one array and it keeps the last call's
+ * contents (each call zeroes the counter first): calls that overlap on the
+ * GPU -- on different streams or from different host threads -- race and
+ * must be serialised by the caller.
  * Limit: n <= RT_NOALLOC_MAX_RAYS per call (the scratch counter is 32-bit);
  * larger n returns RT_EINVAL. */
 #define RT_NOALLOC_SCRATCH_BYTES 256u
@@ -501,6 +504,11 @@ rt_status rt_scene_device_checks(rt_scene* scene, uint32_t* bits, uint32_t* firs
  * a later call on it allocates a new workspace.  No counterpart in the
  * reference. */
 rt_status rt_stream_release(void* stream);
+/* How many per-(device, stream) workspaces the library holds: each is created
+ * with cudaMalloc the first time rt_trace, rt_trace_host, rt_trace_count or
+ * rt_render sees a stream, and freed by rt_stream_release.  A diagnostic of
+ * the library's own device allocations.  No counterpart in the reference. */
+uint32_t rt_workspace_count(void);
 
 #ifdef __cplusplus
 }

@@ -54,7 +54,7 @@ def lib() -> C.CDLL:
         P, U, U64, F, D = C.c_void_p, C.c_uint32, C.c_uint64, C.c_float, C.c_double
         sig = {
             "orc_trace": (C.c_int, [C.POINTER(OScene), P, U, P, U, U, P]),
-            "orc_render": (C.c_int, [C.POINTER(OScene), P, P, U, U, U, U, P, U]),
+            "orc_render": (C.c_int, [C.POINTER(OScene), P, P, U, U, U, U, P, U, U, U]),
             "orc_resolve": (None, [P, U, U, U, P]),
             "orc_build_bvh": (C.c_int, [P, U, P, U, P, U, U, P, P, P, P]),
             "orc_karras": (None, [P, U, P, P]),
@@ -136,12 +136,18 @@ def trace(scene: Scene, rays, any_hit: bool = False, canonical: bool = False, nt
 
 
 def render(scene: Scene, ubo, accum: np.ndarray, width: int, height: int, spp: int, extended: bool = False,
-           background=(0.0, 0.0, 0.0), nthreads: int | None = None) -> int:
-    """accum: float32 [H*W*4], updated in place; returns the status bits."""
+           background=(0.0, 0.0, 0.0), nthreads: int | None = None, rows: tuple[int, int] | None = None,
+           canonical: bool = False) -> int:
+    """accum: float32 [H*W*4], updated in place (only pixel rows
+    rows[0]..rows[1]-1 when given); returns the status bits.  canonical: the
+    culled near-first traversal (same hits except exact ties of t), for
+    frames too large for the reference order."""
     assert accum.dtype == np.float32 and accum.flags["C_CONTIGUOUS"]
     bg = np.asarray(background, np.float32)
-    return lib().orc_render(C.byref(scene.s), C.addressof(ubo), _p(accum), width, height, spp, int(extended),
-                            _p(bg), nthreads if nthreads is not None else threads())
+    y0, y1 = rows if rows is not None else (0, height)
+    flags = (1 if extended else 0) | (2 if canonical else 0)
+    return lib().orc_render(C.byref(scene.s), C.addressof(ubo), _p(accum), width, height, spp, flags,
+                            _p(bg), nthreads if nthreads is not None else threads(), y0, y1)
 
 
 def resolve(accum: np.ndarray, width: int, height: int, spp: int) -> np.ndarray:

@@ -618,14 +618,16 @@ static int scatter(const OScene* S, int extended, v3 d, const ORec* rec, uint32_
 
 /* rayColor, raytraceBVH.comp:276-315 */
 static v3 ray_color(const OScene* S, v3 o, v3 d, uint32_t depth, uint32_t* rng, int extended,
-                    v3 bg, OStats* st) {
+                    v3 bg, int canonical, OStats* st) {
   v3 color = V(0.0f, 0.0f, 0.0f);
   v3 gatt = V(1.0f, 1.0f, 1.0f);
   v3 co = o, cd = vnormalize(d);
   for (uint32_t i = 0; i < depth; ++i) {
     ORec rec;
     memset(&rec, 0, sizeof(rec));
-    if (!hit_bvh_reference(S, co, cd, 0.001f, 10000000.0f, 0, &rec, st, 0)) {
+    int hit = canonical ? hit_bvh_canonical(S, co, cd, 0.001f, 10000000.0f, 0, &rec, st, 0)
+                        : hit_bvh_reference(S, co, cd, 0.001f, 10000000.0f, 0, &rec, st, 0);
+    if (!hit) {
       v3 b = extended ? bg : V(0.0f, 0.0f, 0.0f);
       color = vadd(color, vmul(b, gatt));
       break;
@@ -646,8 +648,8 @@ typedef struct {
   const OScene* S;
   const OUbo* ubo;
   float* accum;
-  uint32_t W, H, spp;
-  int extended;
+  uint32_t W, H, spp, y0, y1;
+  int extended, canonical;
   v3 bg;
   float cam[12];
   _Atomic uint32_t next;
@@ -664,7 +666,7 @@ static void render_pixel(RenderJob* J, uint32_t x, uint32_t y, OStats* st) {
     float next = step_and_output(&rng);
     v3 d = camera_dir(J->cam, x, y);
     v3 o = V(J->cam[0], J->cam[1], J->cam[2]);
-    v3 c = ray_color(J->S, o, d, J->ubo->depth, &rng, J->extended, J->bg, st);
+    v3 c = ray_color(J->S, o, d, J->ubo->depth, &rng, J->extended, J->bg, J->canonical, st);
     px[0] = c.x + px[0];
     px[1] = c.y + px[1];
     px[2] = c.z + px[2];
@@ -676,24 +678,32 @@ static void* render_worker(void* arg) {
   RenderJob* J = (RenderJob*)arg;
   OStats st;
   memset(&st, 0, sizeof(st));
-  uint32_t total = J->W * J->H;
+  uint32_t total = J->W * (J->y1 - J->y0);
   for (;;) {
     uint32_t b = atomic_fetch_add(&J->next, 16u);
     if (b >= total) break;
     uint32_t e = b + 16u < total ? b + 16u : total;
-    for (uint32_t i = b; i < e; ++i) render_pixel(J, i % J->W, i / J->W, &st);
+    for (uint32_t i = b; i < e; ++i) render_pixel(J, i % J->W, J->y0 + i / J->W, &st);
   }
   atomic_fetch_or(&J->status, st.status);
   return NULL;
 }
 
-/* spp samples per pixel into accum (W*H*4 floats, caller-initialised). */
+/* spp samples per pixel into accum (W*H*4 floats, caller-initialised), for
+ * the pixel rows [y0, y1) only (each pixel's samples depend on that pixel
+ * alone, so a band is exactly the band of the whole frame).  flags: bit0 the
+ * extended materials and background, bit1 the canonical (culled, near-first)
+ * traversal instead of the reference order -- the same hits but for exact
+ * ties of t. */
 int orc_render(const OScene* S, const OUbo* ubo, float* accum, uint32_t W, uint32_t H, uint32_t spp,
-               uint32_t extended, const float* bg, uint32_t nthreads) {
+               uint32_t flags, const float* bg, uint32_t nthreads, uint32_t y0, uint32_t y1) {
   RenderJob J;
   memset(&J, 0, sizeof(J));
-  J.S = S; J.ubo = ubo; J.accum = accum; J.W = W; J.H = H; J.spp = spp;
-  J.extended = extended != 0;
+  if (y1 > H) y1 = H;
+  if (y0 > y1) y0 = y1;
+  J.S = S; J.ubo = ubo; J.accum = accum; J.W = W; J.H = H; J.spp = spp; J.y0 = y0; J.y1 = y1;
+  J.extended = (flags & 1u) != 0;
+  J.canonical = (flags & 2u) != 0;
   J.bg = bg ? V(bg[0], bg[1], bg[2]) : V(0.0f, 0.0f, 0.0f);
   orc_camera(ubo, W, H, J.cam);
   atomic_init(&J.next, 0u);

@@ -156,6 +156,7 @@ SIGNATURES = {
     "rt_device_checks_compiled": (_U32, []),
     "rt_scene_device_checks": (_I, [_P, C.POINTER(_U32), C.POINTER(_U32)]),
     "rt_stream_release": (_I, [_P]),
+    "rt_workspace_count": (_U32, []),
     "rt_pool_create": (_I, [C.POINTER(PoolOptions), C.POINTER(C.c_void_p)]),
     "rt_pool_destroy": (_I, [_P]),
     "rt_pool_add_scene": (_I, [_P, C.POINTER(_SceneDesc), C.POINTER(_U32)]),
@@ -561,6 +562,11 @@ class Server:
 def device_checks_compiled() -> bool:
     """True for the checked build (RT_DEVICE_CHECKS=1)."""
     return bool(lib().rt_device_checks_compiled())
+
+
+def workspace_count() -> int:
+    """Per-(device, stream) workspaces the library holds (each made by cudaMalloc)."""
+    return int(lib().rt_workspace_count())
 
 
 def release_stream(stream=None) -> None:

@@ -214,6 +214,11 @@ rt_status rt_scene_device_checks(rt_scene* scene, uint32_t* bits, uint32_t* firs
   return RT_OK;
 }
 
+uint32_t rt_workspace_count(void) {
+  std::lock_guard<std::mutex> lk(g_ws_mu);
+  return (uint32_t)g_ws.size();
+}
+
 rt_status rt_stream_release(void* stream) {
   cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
   int dev = 0;
@@ -606,10 +611,17 @@ rt_status rt_trace_host(rt_scene* scene, const RtRay* h_rays, uint32_t n, RtHit*
   cudaEvent_t* out_done = &w->ev[4];
   // buffers b are free again once chunk c-2 is traced (direct) or downloaded
   cudaEvent_t* free_again = direct ? trace_done : out_done;
+  // Every error return from here on first waits for the helper streams and
+  // the caller's stream: nothing this call enqueued may still touch h_rays
+  // or h_hits after it returns.
+  auto drain = [&](rt_status rs) {
+    for (cudaStream_t h : {w->copy_in, w->trace2, w->copy_out, st}) cudaStreamSynchronize(h);
+    return rs;
+  };
   // the caller's earlier work on `stream` comes first (trace2 follows it
   // through copy_in's events)
-  if ((e = cudaEventRecord(w->ev[6], st)) != cudaSuccess) return cuda_fail(e, "event");
-  if ((e = cudaStreamWaitEvent(w->copy_in, w->ev[6], 0)) != cudaSuccess) return cuda_fail(e, "wait");
+  if ((e = cudaEventRecord(w->ev[6], st)) != cudaSuccess) return drain(cuda_fail(e, "event"));
+  if ((e = cudaStreamWaitEvent(w->copy_in, w->ev[6], 0)) != cudaSuccess) return drain(cuda_fail(e, "wait"));
   uint32_t chunks = 0;
   auto enqueue = [&]() -> rt_status {
     uint32_t size = std::min(chunk, kFirstChunk);
@@ -643,24 +655,20 @@ rt_status rt_trace_host(rt_scene* scene, const RtRay* h_rays, uint32_t n, RtHit*
     }
     return RT_OK;
   };
-  if ((s = enqueue()) != RT_OK) {
-    // nothing this call enqueued may still touch h_rays or h_hits after it
-    // returns: wait for the helper streams and the caller's stream
-    for (cudaStream_t h : {w->copy_in, w->trace2, w->copy_out, st}) cudaStreamSynchronize(h);
-    return s;
-  }
+  if ((s = enqueue()) != RT_OK) return drain(s);
   if (direct) {
     // the caller's stream continues after trace2's last chunk; its own chunks
     // are already in order on it
-    if (chunks >= 2 && (e = cudaStreamWaitEvent(st, trace_done[1], 0)) != cudaSuccess) return cuda_fail(e, "wait");
-    if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return cuda_fail(e, "rt_trace_host: sync");
+    if (chunks >= 2 && (e = cudaStreamWaitEvent(st, trace_done[1], 0)) != cudaSuccess)
+      return drain(cuda_fail(e, "wait"));
+    if ((e = cudaStreamSynchronize(st)) != cudaSuccess) return drain(cuda_fail(e, "rt_trace_host: sync"));
     return RT_OK;
   }
   // the caller's stream continues after the last download (every chunk's
   // download waited for its trace, so trace2 is drained too)
-  if ((e = cudaEventRecord(w->ev[7], w->copy_out)) != cudaSuccess) return cuda_fail(e, "event");
-  if ((e = cudaStreamWaitEvent(st, w->ev[7], 0)) != cudaSuccess) return cuda_fail(e, "wait");
-  if ((e = cudaStreamSynchronize(w->copy_out)) != cudaSuccess) return cuda_fail(e, "rt_trace_host: sync");
+  if ((e = cudaEventRecord(w->ev[7], w->copy_out)) != cudaSuccess) return drain(cuda_fail(e, "event"));
+  if ((e = cudaStreamWaitEvent(st, w->ev[7], 0)) != cudaSuccess) return drain(cuda_fail(e, "wait"));
+  if ((e = cudaStreamSynchronize(w->copy_out)) != cudaSuccess) return drain(cuda_fail(e, "rt_trace_host: sync"));
   return RT_OK;
 }
 

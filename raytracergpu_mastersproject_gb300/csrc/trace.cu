@@ -380,8 +380,8 @@ cudaError_t launch_trace_raw(const DeviceScene& S, const float4* rays, uint32_t 
 
 // ---- allocation-free ray queries (rt_trace_noalloc) ----
 // Scratch of rt_trace_noalloc: word 0 is the persistent kernel's ray-queue
-// counter, word 1 a status word.  Every device that loads the library holds
-// this array until the process exits; all calls share it.
+// counter; the rest of the array is unused.  Every device that loads the
+// library holds this array until the process exits; all calls share it.
 static __device__ __align__(256) uint32_t g_noalloc_scratch[RT_NOALLOC_SCRATCH_BYTES / sizeof(uint32_t)];
 
 namespace {
@@ -436,9 +436,9 @@ extern "C" rt_status rt_trace_noalloc(rt_scene* scene, const RtRay* d_rays, uint
     scratch = g_noalloc_ptr[dev];
   }
   cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
-  // The array keeps the previous call's contents: the queue counter and the
-  // status word must start at zero.
-  e = cudaMemsetAsync(scratch, 0, 2 * sizeof(uint32_t), st);
+  // The array keeps the previous call's contents: the queue counter must
+  // start at zero.
+  e = cudaMemsetAsync(scratch, 0, sizeof(uint32_t), st);
   if (e != cudaSuccess) {
     set_error(std::string("rt_trace_noalloc: memset: ") + cudaGetErrorString(e));
     return RT_ECUDA;

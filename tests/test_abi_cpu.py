@@ -30,7 +30,7 @@ def test_every_declared_symbol_is_exported(rt):
     L = rt.lib()
     missing = [n for n in names if not hasattr(L, n)]
     assert not missing, missing
-    assert set(rt.SIGNATURES) <= set(names) | {"rt_trace_noalloc"}
+    assert set(rt.SIGNATURES) <= set(names)
 
 
 def test_abi_version_and_record_sizes(rt):

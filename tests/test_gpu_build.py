@@ -1,5 +1,6 @@
 """The GPU LBVH build (rt_build_bvh_device) must emit exactly the node array
-of the host build (and so of the oracle's transcription of the six S1 passes)."""
+of the oracle's transcription of the six S1 passes (ModelSpaceToWorldSpace.comp
+to ConstructAABBsOfInternalNodes.comp), and of the host build."""
 import numpy as np
 import pytest
 
@@ -46,3 +47,29 @@ def test_device_build_config3_and_scene(rt, cuda):
     assert np.array_equal(device_build(rt, cuda, tris).view(np.uint8), host.view(np.uint8))
     with rt.Scene(tris[:200_000], build_on_device=True) as a, rt.Scene(tris[:200_000]) as b:
         assert np.array_equal(a.nodes().view(np.uint8), b.nodes().view(np.uint8))
+
+
+@pytest.mark.parametrize("mode", [0, 1], ids=["sorted", "reference"])
+def test_device_build_matches_oracle(rt, orc, cuda, mode):
+    """The device build against the oracle's transcription of the S1 passes
+    (which the CPU suite pins to the reference's own shaders in reference
+    mode): config 1, a soup with spheres, duplicate centroids, the full
+    config-3 soup, and sizes around the device kernels' block sizes."""
+    tris, _, _ = rt.gen_config1()
+    assert np.array_equal(device_build(rt, cuda, tris, mode=mode).view(np.uint8),
+                          orc.build_bvh(tris, mode=mode)[0].view(np.uint8))
+    soup = rt.gen_soup(8, 0, 200_000, 1.0, 0.002)
+    sph = np.zeros(40, rt.SPHERE_DTYPE)
+    sph["center"][:, :3] = np.random.default_rng(8).random((40, 3)).astype(np.float32)
+    sph["radius"] = np.float32(0.01)
+    assert np.array_equal(device_build(rt, cuda, soup, sph, mode).view(np.uint8),
+                          orc.build_bvh(soup, spheres=sph, mode=mode)[0].view(np.uint8))
+    dup = np.concatenate([soup[:500]] * 6)
+    assert np.array_equal(device_build(rt, cuda, dup, mode=mode).view(np.uint8),
+                          orc.build_bvh(dup, mode=mode)[0].view(np.uint8))
+    for n in (1, 2, 255, 256, 257, 1023, 1025):
+        assert np.array_equal(device_build(rt, cuda, soup[:n], mode=mode).view(np.uint8),
+                              orc.build_bvh(soup[:n], mode=mode)[0].view(np.uint8)), n
+    big = rt.gen_soup(3, 0, 4_194_304, 1.0, 0.002)
+    assert np.array_equal(device_build(rt, cuda, big, mode=mode).view(np.uint8),
+                          orc.build_bvh(big, mode=mode)[0].view(np.uint8))

@@ -56,6 +56,34 @@ def test_reference_shading(rt, orc, cuda, mode, width):
     assert img[0::4].max() > 0.1       # the light reaches the camera
 
 
+def test_config2_frame(rt, orc, cuda):
+    """Config 2's own frame, built as the bench builds it: 64 displaced
+    subdiv-6 icospheres (5,242,880 triangles) with lambertian, metal and glass
+    materials, camera (0,3,28) -> 0, FOV 40, 1280x720, 16 spp, depth 8.  Both
+    shadings, with the first hit shared by a pixel's samples (the default) and
+    with every sample's primary ray traced, against the oracle's whole frame
+    (raytraceBVH.comp:276-315, 345-375 in the reference's traversal order)."""
+    tris, mats = rt.gen_spheres_scene(2, 64, 6, 0.05)
+    assert len(tris) == 5_242_880
+    w, h, spp = 1280, 720, 16
+    ubo = rt.make_ubo((0.0, 3.0, 28.0), (0.0, 0.0, 0.0), fov=40.0, depth=8, random_state=2,
+                      num_triangles=len(tris), num_materials=len(mats))
+    bg = (0.6, 0.7, 1.0)
+    with rt.Scene(tris, materials=mats) as sc:
+        nodes = sc.nodes()
+        for mode, ext in ((rt.SHADE_EXTENDED, True), (rt.SHADE_REFERENCE, False)):
+            imgs = [gpu_render(rt, cuda, sc, ubo, w, h, spp, shade_mode=mode, background=bg,
+                               trace_every_primary=every) for every in (False, True)]
+            ref = oracle_render(orc, tris, nodes, mats, ubo, w, h, spp, extended=ext, background=bg)
+            assert np.array_equal(imgs[0], imgs[1])  # sharing the first hit changes nothing
+            img = imgs[0]
+            assert rmse(img, ref) <= 1e-3
+            assert np.mean(np.all(img.reshape(-1, 4) == ref.reshape(-1, 4), axis=1)) > 0.98
+            assert np.array_equal(img[3::4].view(np.uint32), ref[3::4].view(np.uint32))  # alpha RNG carry
+            if ext:
+                assert img[0::4].mean() / spp > 0.2  # sky and lit spheres, not a black frame
+
+
 def test_samples_split_across_calls(rt, cuda):
     """Alpha carries the RNG between samples (raytraceBVH.comp:350-372), so
     two calls of 2 samples equal one call of 4."""

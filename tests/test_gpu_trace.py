@@ -92,7 +92,9 @@ def test_any_hit_semantics(rt, orc, cuda, width):
 
 def test_config3_full_size(rt, orc, cuda):
     """4,194,304 triangles, 16,777,216 rays: every ray against the oracle's
-    canonical traversal; any-hit agrees with closest-hit on which rays hit;
+    canonical traversal, and the first 2,097,152 against the reference's own
+    order (push left, go right, no culling: raytraceBVH.comp:236-244) with
+    binary64 arbitration; any-hit agrees with closest-hit on which rays hit;
     a second run is bit-identical."""
     tris = rt.gen_soup(3, 0, 4_194_304, 1.0, 0.002)
     rays = rt.gen_rays(3, 0, 16_777_216, 1.0, 1e-4, float("inf"))
@@ -106,8 +108,11 @@ def test_config3_full_size(rt, orc, cuda):
     can, _ = orc.trace(S, rays, canonical=True)
     arb = assert_parity(orc, tris, rays, can, got)
     assert arb["mismatch"] < 1000
-    ref, _ = orc.trace(S, rays[:8192])
-    assert_parity(orc, tris, rays[:8192], ref, got[:8192])
+    k = 2_097_152
+    ref, st = orc.trace(S, rays[:k])
+    assert st[4] == 0
+    arb = assert_parity(orc, tris, rays[:k], ref, got[:k])
+    assert arb["mismatch"] < 200
 
 
 def test_trace_host_matches_device(rt, cuda):
