@@ -65,12 +65,14 @@ def parse():
     p.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-sort", action="store_true", help="trace in the given ray order (no RT_TRACE_SORT)")
+    p.add_argument("--no-tune", action="store_true", help="skip rt_trace_autotune (default launch)")
     p.add_argument("--no-batched", action="store_true", help="skip the config-4 batched comparison")
     p.add_argument("--no-served", action="store_true", help="skip the config-5 serving run")
     p.add_argument("--no-render", action="store_true", help="skip the config-2 path-tracing run")
     p.add_argument("--render-spp", type=int, default=16, help="samples per pixel of the config-2 frame")
     p.add_argument("--serve-requests", type=int, default=200)
-    p.add_argument("--serve-rates", type=str, default="1000,4000,8000", help="Poisson arrival rates (requests/s)")
+    p.add_argument("--serve-rates", type=str, default="250,500,1000,2000,4000,8000,16000",
+                   help="Poisson arrival rates (requests/s), swept in order")
     return p.parse_args()
 
 
@@ -281,6 +283,7 @@ def run_batched(torch, rt) -> dict:
     torch.cuda.synchronize()
     same = all(torch.equal(a, b) for a, b in zip(dh_plain, dh_batch))
     thr, minb, ring = rt.describe_pool_variant(variant)
+    pinfo = pool.info()
     out = {"workload": "config 4: 256 triangle soups, counts log-uniform in [1K, 256K], each with a ray batch "
                        "log-uniform in [4K, 1M] rays, closest-hit",
            "triangles": nt, "rays": nr, "unit": UNIT,
@@ -289,7 +292,9 @@ def run_batched(torch, rt) -> dict:
            "batched": {"value": nr / ms_batch / 1e6, "ms": ms_batch, "launches": 1, "cuda_graph": True,
                        "untuned_ms": ms_untuned,
                        "autotuned": {"threads_per_block": thr, "min_blocks_per_sm": minb,
-                                     "stack_entries_in_shared_memory": ring, "refill": refill}},
+                                     "stack_entries_in_shared_memory": ring, "refill": refill,
+                                     "stack_entries": int(pinfo.tuned_stack),
+                                     "tile_nodes_per_scene": int(pinfo.tuned_tile)}},
            "speedup": ms_plain / ms_batch, "identical_hits": bool(same)}
     pool.close()
     for sc in scenes:
@@ -363,6 +368,39 @@ def run_render(torch, rt, spp: int = 16) -> dict:
     return out
 
 
+def sustained(m: dict) -> bool:
+    """A rate is sustained when the queue does not build up over the run: the
+    later third of the queries wait at most twice as long (plus 2 ms) as the
+    first third, and queries complete at least at 80 % of the offered rate."""
+    return bool(m["late_over_early_p50"] <= 2.0 + 2.0 / max(m["p50_ms"], 1e-3)
+                and m["completed_queries_per_s"] >= 0.8 * m["offered_queries_per_s"])
+
+
+def serving_summary(runs: list[dict]) -> dict:
+    """Per mode the highest swept rate it sustains (with every lower rate), and
+    the latencies of both modes at the highest rate both sustain."""
+    out = {}
+    for mode in ("batched", "sequential"):
+        best = None
+        for r in runs:
+            if not r[mode]["sustained"]:
+                break
+            best = r["rate_per_s"]
+        out[f"{mode}_max_sustained_req_per_s"] = best
+    both = [r for r in runs if r["batched"]["sustained"] and r["sequential"]["sustained"]]
+    if both:
+        r = both[-1]
+        out["at_rate_both_sustain"] = {"rate_per_s": r["rate_per_s"],
+                                       "batched_p50_p99_ms": [round(r["batched"]["p50_ms"], 3), round(r["batched"]["p99_ms"], 3)],
+                                       "sequential_p50_p99_ms": [round(r["sequential"]["p50_ms"], 3),
+                                                                 round(r["sequential"]["p99_ms"], 3)]}
+    out["p99_ms_by_rate"] = {str(int(r["rate_per_s"])): [round(r["batched"]["p99_ms"], 2), round(r["sequential"]["p99_ms"], 2)]
+                             for r in runs}
+    out["Grays_by_rate"] = {str(int(r["rate_per_s"])): [round(r["batched"]["Grays_per_s"], 3),
+                                                        round(r["sequential"]["Grays_per_s"], 3)] for r in runs}
+    return out
+
+
 def run_served(torch, rt, n_requests: int, rates: list[float]) -> dict:
     """Config 5: 64 resident scenes, Poisson arrivals; 90% ray queries
     (log-uniform [1K, 2M] rays, closest-hit), 10% new-scene uploads; latency
@@ -421,11 +459,17 @@ def run_served(torch, rt, n_requests: int, rates: list[float]) -> dict:
             for sid in new_scenes:
                 srv.remove_scene(sid)
             lat_ms = np.array(lat) * 1e3
+            arr = np.array([rq[0] for rq in reqs if rq[1] == "rays"])
+            third = max(1, len(lat_ms) // 3)
             entry[mode] = {"p50_ms": float(np.percentile(lat_ms, 50)), "p99_ms": float(np.percentile(lat_ms, 99)),
                            "mean_ms": float(lat_ms.mean()), "rays_per_s": tot_rays / wall,
                            "Grays_per_s": tot_rays / wall / 1e9, "query_span_s": wall,
+                           "offered_queries_per_s": len(arr) / max(float(arr[-1] - arr[0]), 1e-9),
+                           "completed_queries_per_s": len(arr) / wall,
+                           "late_over_early_p50": float(np.median(lat_ms[-third:]) / max(np.median(lat_ms[:third]), 1e-6)),
                            "mean_queries_per_launch": float(np.mean(batch_jobs)),
                            "upload_p50_s": float(np.median(up_lat)) if up_lat else None}
+            entry[mode]["sustained"] = sustained(entry[mode])
         runs.append(entry)
     st = srv.stats()
     srv.close()
@@ -433,6 +477,7 @@ def run_served(torch, rt, n_requests: int, rates: list[float]) -> dict:
                         "90% closest-hit queries of log-uniform [1K, 2M] rays from pinned host memory, "
                         "10% new-scene uploads (BVH built on the GPU); HBM budget 150 GB",
             "resident_triangles": res_tris, "setup_s": setup_s, "runs": runs,
+            "summary": serving_summary(runs),
             "batches_total": int(st.batches), "evictions": int(st.evictions),
             "latency": "submit of the host request to its hits back in host memory",
             "sequential": "same server, one query per launch, one launch at a time"}
@@ -534,6 +579,10 @@ def run_ours(args):
     for _ in range(args.warmup):
         scene.trace(d_rays, d_hits, sort=sort)
     torch.cuda.synchronize()
+    # rt_trace_autotune on this batch: launch shape, refill, stack capacity and
+    # staged top-of-tree tile; the timed steps run with what it keeps
+    tuned = None if args.no_tune else scene.autotune(d_rays, d_hits, sort=sort, repeats=2).as_dict()
+    torch.cuda.synchronize()
     gpu_nodes, gpu_tests = scene.trace_count(d_rays, d_hits, sort=sort)
     clocks = ClockSampler(local)
     clocks.start()
@@ -629,11 +678,28 @@ def run_ours(args):
                        "device_nodes": info.device_nodes, "bvh_depth": info.depth, "stack_need": info.stack_need,
                        "l2": l2_note(n, info),
                        "ray_order": "origin-bucketed inside the step (RT_TRACE_SORT)" if sort else "as given",
+                       "launch": tuned if tuned else "default (not tuned)",
                        "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU"},
             "roofline": roof, "cpu_baseline": cpu_base, "e2e": e2e, "clocks": clk,
             "batched": batched, "served": served, "render": render, "extras": extras,
             "gpu_launches": args.steps * (4 if sort else 1), "parity_sample": parity,
             "scene_build_s": info.build_seconds}
+    # the headline figures of the long blocks above, last on the line, so
+    # that a tail of the output still holds them
+    summary = {}
+    if tuned:
+        summary["launch_config3"] = {k: (round(v, 3) if isinstance(v, float) else v) for k, v in tuned.items()}
+    if batched:
+        summary["batched_config4"] = {"plain_Grays_per_s": round(batched["plain"]["value"], 3),
+                                      "batched_Grays_per_s": round(batched["batched"]["value"], 3),
+                                      "speedup": round(batched["speedup"], 3), "identical_hits": batched["identical_hits"],
+                                      "autotuned": batched["batched"]["autotuned"]}
+    if render:
+        summary["render_config2_Mpaths_per_s"] = {"extended": round(render["extended"]["value"], 1),
+                                                  "reference": round(render["reference"]["value"], 1)}
+    if served:
+        summary["served_config5"] = served["summary"]
+    line["summary"] = summary
     print(json.dumps(line), flush=True)
     if dist is not None:
         dist.destroy_process_group()

@@ -268,6 +268,30 @@ rt_status rt_trace_host(rt_scene* scene, const RtRay* h_rays, uint32_t n, RtHit*
 rt_status rt_trace_count(rt_scene* scene, const RtRay* d_rays, uint32_t n, RtHit* d_hits, uint32_t flags,
                          void* stream, uint64_t* h_counts);
 
+/* The launch of rt_trace / rt_trace_host for one scene.  No counterpart in the
+ * reference, whose dispatch size is fixed (RaytracerBVH.cpp:1025-1050). */
+typedef struct RtTraceTuning {
+  uint32_t launch_shape;   /* ray-query launch shape (threads per block x resident blocks,
+                              traversal-stack ring in shared memory); index into the
+                              table RT_TRACE_VARIANT selects from */
+  uint32_t refill;         /* idle lanes of a warp that make it take new rays */
+  uint32_t stack_entries;  /* traversal stack capacity per lane (>= the tree's worst case) */
+  uint32_t tile_nodes;     /* top-of-tree nodes staged in shared memory per block (0: none) */
+  float best_ms;           /* rt_trace_autotune: the best launch time measured */
+} RtTraceTuning;
+/* Times rt_trace's launch shapes, refill thresholds, stack capacities and
+ * top-of-tree staging tiles on the caller's batch (flags RT_TRACE_ANY and
+ * RT_TRACE_SORT as for rt_trace), keeps the fastest for the scene (used by
+ * later rt_trace and rt_trace_host calls; hits do not depend on it) and
+ * reports it in *out (may be NULL).  d_hits receives the batch's hits.
+ * Synchronous; launches each candidate 1 + repeats times (repeats 0: 3). */
+rt_status rt_trace_autotune(rt_scene* scene, const RtRay* d_rays, uint32_t n, RtHit* d_hits, uint32_t flags,
+                            void* stream, uint32_t repeats, RtTraceTuning* out);
+rt_status rt_scene_get_tuning(const rt_scene* scene, RtTraceTuning* out);
+/* RT_EINVAL when the scene cannot run the given launch (an unknown shape, a
+ * stack capacity below the tree's worst case, a tile on a shape without one). */
+rt_status rt_scene_set_tuning(rt_scene* scene, const RtTraceTuning* tuning);
+
 /* rt_trace without any device allocation.  No counterpart in the reference.
  *
  * Who needs it: host applications that must not call cudaMalloc while they
@@ -321,6 +345,8 @@ typedef struct RtPoolInfo {
   uint32_t num_triangles;
   uint32_t tuned_variant; /* launch shape in use (see rt_pool_describe_variant) */
   int32_t tuned_refill;   /* idle lanes that trigger a ray refill */
+  uint32_t tuned_stack;   /* traversal stack capacity per lane */
+  uint32_t tuned_tile;    /* top-of-tree nodes of each job's scene staged in shared memory (0: none) */
   uint32_t _pad;
 } RtPoolInfo;
 
@@ -345,10 +371,20 @@ rt_status rt_pool_get_info(const rt_pool* pool, RtPoolInfo* out_info);
  * identical to rt_trace on each scene alone. */
 rt_status rt_pool_trace(rt_pool* pool, const RtJob* jobs, uint32_t num_jobs, uint32_t flags, void* stream);
 /* Times the jobs under every launch shape (threads per block, register cap)
- * and refill threshold, `repeats` launches each, and keeps the fastest for
- * later rt_pool_trace calls.  Synchronous. */
+ * and refill threshold, then, on the two shapes of 128 threads x 10 blocks,
+ * every traversal stack capacity (48, 64, 96, 192 entries, at least the pooled
+ * scenes' worst case) and top-of-tree tile (0, 1 or 2 nodes of each job's
+ * scene staged in shared memory per block, for batches of up to 256 jobs),
+ * `repeats` launches each, and keeps the fastest for later rt_pool_trace
+ * calls (rt_pool_get_info reports it).  Synchronous. */
 rt_status rt_pool_autotune(rt_pool* pool, const RtJob* jobs, uint32_t num_jobs, uint32_t flags, void* stream,
                            uint32_t repeats);
+/* Sets the launch rt_pool_trace uses (what rt_pool_autotune would choose):
+ * launch shape, refill threshold, stack capacity (0: 64 or 192 by the pooled
+ * scenes' worst case) and top-of-tree tile per job (0, 1 or 2; variants 0
+ * and 3 only).  RT_EINVAL for a combination the pool cannot run. */
+rt_status rt_pool_set_tuning(rt_pool* pool, uint32_t variant, int32_t refill, uint32_t stack_entries,
+                             uint32_t tile_nodes);
 /* Launch shape of a variant: threads per block, minimum resident blocks per
  * SM (the register cap), and the traversal-stack entries kept in shared
  * memory per lane (0: all in local memory).  stack_ring may be NULL. */

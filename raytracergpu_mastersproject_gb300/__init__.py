@@ -67,6 +67,16 @@ class RaytracingUBO(C.Structure):
                 ("randomState", C.c_uint32), ("_pad", C.c_uint32)]
 
 
+class TraceTuning(C.Structure):
+    """RtTraceTuning: the launch of rt_trace / rt_trace_host for one scene."""
+    _fields_ = [("launch_shape", C.c_uint32), ("refill", C.c_uint32), ("stack_entries", C.c_uint32),
+                ("tile_nodes", C.c_uint32), ("best_ms", C.c_float)]
+
+    def as_dict(self) -> dict:
+        return {"launch_shape": self.launch_shape, "refill": self.refill, "stack_entries": self.stack_entries,
+                "tile_nodes": self.tile_nodes, "best_ms": self.best_ms}
+
+
 class _SceneDesc(C.Structure):
     _fields_ = [("triangles", C.c_void_p), ("num_triangles", C.c_uint32), ("spheres", C.c_void_p),
                 ("num_spheres", C.c_uint32), ("materials", C.c_void_p), ("num_materials", C.c_uint32),
@@ -93,7 +103,8 @@ class PoolOptions(C.Structure):
 class PoolInfo(C.Structure):
     _fields_ = [("num_scenes", C.c_uint32), ("stack_need", C.c_uint32), ("used_bytes", C.c_uint64),
                 ("budget_bytes", C.c_uint64), ("arena_bytes", C.c_uint64), ("num_triangles", C.c_uint32),
-                ("tuned_variant", C.c_uint32), ("tuned_refill", C.c_int32), ("_pad", C.c_uint32)]
+                ("tuned_variant", C.c_uint32), ("tuned_refill", C.c_int32), ("tuned_stack", C.c_uint32),
+                ("tuned_tile", C.c_uint32), ("_pad", C.c_uint32)]
 
 
 class Job(C.Structure):
@@ -157,6 +168,9 @@ SIGNATURES = {
     "rt_scene_device_checks": (_I, [_P, C.POINTER(_U32), C.POINTER(_U32)]),
     "rt_stream_release": (_I, [_P]),
     "rt_workspace_count": (_U32, []),
+    "rt_trace_autotune": (_I, [_P, _P, _U32, _P, _U32, _P, _U32, C.POINTER(TraceTuning)]),
+    "rt_scene_get_tuning": (_I, [_P, C.POINTER(TraceTuning)]),
+    "rt_scene_set_tuning": (_I, [_P, C.POINTER(TraceTuning)]),
     "rt_pool_create": (_I, [C.POINTER(PoolOptions), C.POINTER(C.c_void_p)]),
     "rt_pool_destroy": (_I, [_P]),
     "rt_pool_add_scene": (_I, [_P, C.POINTER(_SceneDesc), C.POINTER(_U32)]),
@@ -165,6 +179,7 @@ SIGNATURES = {
     "rt_pool_trace": (_I, [_P, C.POINTER(Job), _U32, _U32, _P]),
     "rt_pool_autotune": (_I, [_P, C.POINTER(Job), _U32, _U32, _P, _U32]),
     "rt_pool_describe_variant": (_I, [_U32, C.POINTER(_U32), C.POINTER(_U32), C.POINTER(_U32)]),
+    "rt_pool_set_tuning": (_I, [_P, _U32, C.c_int32, _U32, _U32]),
     "rt_server_create": (_I, [C.POINTER(ServerOptions), C.POINTER(C.c_void_p)]),
     "rt_server_destroy": (_I, [_P]),
     "rt_server_upload": (_I, [_P, C.POINTER(_SceneDesc), C.POINTER(_U64)]),
@@ -299,6 +314,25 @@ class Scene:
         flags = (TRACE_ANY if any_hit else TRACE_CLOSEST) | (TRACE_SORT if sort else 0) | (TRACE_MT if mt else 0)
         _check(lib().rt_trace(self.handle, _ptr(rays), n, _ptr(hits), flags, _stream_handle(stream)), "rt_trace")
 
+    def autotune(self, rays, hits, n: int | None = None, any_hit: bool = False, sort: bool = False, stream=None,
+                 repeats: int = 3) -> TraceTuning:
+        """rt_trace_autotune: times the launch options on this batch and keeps the fastest."""
+        if n is None:
+            n = rays.numel() * rays.element_size() // RAY_DTYPE.itemsize
+        flags = (TRACE_ANY if any_hit else TRACE_CLOSEST) | (TRACE_SORT if sort else 0)
+        out = TraceTuning()
+        _check(lib().rt_trace_autotune(self.handle, _ptr(rays), n, _ptr(hits), flags, _stream_handle(stream),
+                                       repeats, C.byref(out)), "rt_trace_autotune")
+        return out
+
+    def tuning(self) -> TraceTuning:
+        out = TraceTuning()
+        _check(lib().rt_scene_get_tuning(self.handle, C.byref(out)), "rt_scene_get_tuning")
+        return out
+
+    def set_tuning(self, t: TraceTuning) -> None:
+        _check(lib().rt_scene_set_tuning(self.handle, C.byref(t)), "rt_scene_set_tuning")
+
     def trace_count(self, rays, hits, n: int | None = None, any_hit: bool = False, sort: bool = False,
                     stream=None) -> tuple[int, int]:
         """rt_trace with work counters -> (inner nodes fetched, primitives tested)."""
@@ -425,11 +459,15 @@ class Pool:
                                    _stream_handle(stream)), "rt_pool_trace")
 
     def autotune(self, jobs, any_hit: bool = False, repeats: int = 3, stream=None) -> tuple[int, int]:
+        """-> (launch shape, refill); info() also reports the stack capacity and tile chosen."""
         arr = self._jobs(jobs)
         _check(lib().rt_pool_autotune(self.handle, arr, len(jobs), TRACE_ANY if any_hit else TRACE_CLOSEST,
                                       _stream_handle(stream), repeats), "rt_pool_autotune")
         inf = self.info()
         return inf.tuned_variant, inf.tuned_refill
+
+    def set_tuning(self, variant: int, refill: int, stack_entries: int = 0, tile_nodes: int = 0) -> None:
+        _check(lib().rt_pool_set_tuning(self.handle, variant, refill, stack_entries, tile_nodes), "rt_pool_set_tuning")
 
     def render_count(self, ubo: RaytracingUBO, accum, width: int, height: int, spp: int,
                      shade_mode: int = SHADE_REFERENCE, background=(0.0, 0.0, 0.0), stream=None,

@@ -29,6 +29,7 @@ struct rt_scene {
   RtSceneInfo info{};
   uint32_t max_material = 0;  // largest material index referenced (+1), 0 if none
   int device = 0;
+  rtgb::TraceTuning tune = rtgb::default_tuning();  // launch of rt_trace / rt_trace_host (rt_trace_autotune)
 };
 
 namespace rtgb {
@@ -502,7 +503,8 @@ rt_status rt_trace(rt_scene* scene, const RtRay* d_rays, uint32_t n, RtHit* d_hi
   if ((s = maybe_reorder(w, scene->d, d_rays, n, flags, st, &order)) != RT_OK) return s;
   cudaError_t e = cudaMemsetAsync(w->counters, 0, 2 * sizeof(uint32_t), st);
   if (e != cudaSuccess) return cuda_fail(e, "rt_trace: memset");
-  e = launch_trace(scene->d, d_rays, n, d_hits, flags, w->counters, stream, order);
+  e = launch_trace_tuned(scene->d, d_rays, n, d_hits, flags, w->counters, stream,
+                         (flags & RT_TRACE_MT) ? default_tuning() : scene->tune, nullptr, order);
   if (e != cudaSuccess) return cuda_fail(e, "rt_trace: launch");
   return RT_OK;
 }
@@ -534,6 +536,122 @@ rt_status rt_trace_count(rt_scene* scene, const RtRay* d_rays, uint32_t n, RtHit
   if (e != cudaSuccess) return cuda_fail(e, "rt_trace_count: read counters");
   h_counts[0] = hc[0];
   h_counts[1] = hc[1];
+  return RT_OK;
+}
+
+rt_status rt_trace_autotune(rt_scene* scene, const RtRay* d_rays, uint32_t n, RtHit* d_hits, uint32_t flags,
+                            void* stream, uint32_t repeats, RtTraceTuning* out) {
+  rtgb::NvtxRange nvtx_range("rt_trace_autotune");
+  if (!scene || !d_rays || !d_hits || n == 0 || n > 0x80000000u || (flags & ~(uint32_t)(RT_TRACE_ANY | RT_TRACE_SORT))) {
+    set_error("rt_trace_autotune: bad argument (rays and hits required; flags RT_TRACE_ANY / RT_TRACE_SORT)");
+    return RT_EINVAL;
+  }
+  if (repeats == 0) repeats = 3;
+  cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+  Workspace* w = nullptr;
+  rt_status s = workspace(st, &w);
+  if (s != RT_OK) return s;
+  uint32_t* order = nullptr;
+  if ((s = maybe_reorder(w, scene->d, d_rays, n, flags, st, &order)) != RT_OK) return s;
+  cudaEvent_t a = nullptr, b = nullptr;
+  cudaError_t e = cudaEventCreate(&a);
+  if (e == cudaSuccess) e = cudaEventCreate(&b);
+  if (e != cudaSuccess) return cuda_fail(e, "rt_trace_autotune: events");
+  // one warm-up launch, then `repeats` timed launches of one candidate
+  auto time_one = [&](const TraceTuning& t, float* ms) -> cudaError_t {
+    cudaError_t r = cudaSuccess;
+    for (uint32_t k = 0; k <= repeats && r == cudaSuccess; ++k) {
+      if (k == 1) r = cudaEventRecord(a, st);
+      if (r == cudaSuccess) r = cudaMemsetAsync(w->counters, 0, 2 * sizeof(uint32_t), st);
+      if (r == cudaSuccess) r = launch_trace_tuned(scene->d, d_rays, n, d_hits, flags, w->counters, stream, t, nullptr, order);
+    }
+    if (r == cudaSuccess) r = cudaEventRecord(b, st);
+    if (r == cudaSuccess) r = cudaEventSynchronize(b);
+    if (r == cudaSuccess) r = cudaEventElapsedTime(ms, a, b);
+    if (r == cudaSuccess) *ms /= (float)repeats;
+    return r;
+  };
+  TraceTuning best = scene->tune;
+  float best_ms = 3.4e38f;
+  auto consider = [&](const TraceTuning& t) -> cudaError_t {
+    if (!tuning_supported(t, scene->d.width, scene->d.stack_need, flags)) return cudaSuccess;
+    float ms = 0.0f;
+    const cudaError_t r = time_one(t, &ms);
+    if (r == cudaSuccess && ms < best_ms) {
+      best_ms = ms;
+      best = t;
+    }
+    return r;
+  };
+  // 1. launch shape x refill threshold; 2. at the default shape, the stack
+  // capacity and the top-of-tree staging tile.
+  static const int shapes[] = {kTunedVariant, 7, 3, 4};
+  static const int refills[] = {3, 5, 8};
+  TraceTuning t = default_tuning();
+  t.stack = 0;
+  t.tile = 0;
+  e = consider(scene->tune);
+  for (int v : shapes)
+    for (int r : refills) {
+      if (e != cudaSuccess) break;
+      t.variant = v;
+      t.refill = r;
+      e = consider(t);
+    }
+  if (e == cudaSuccess && best.variant == kTunedVariant && scene->d.width == 4) {
+    t = best;
+    for (int sc : kTunedStacks)
+      for (int tl : kTunedTiles) {
+        if (e != cudaSuccess) break;
+        t.stack = sc;
+        t.tile = tl;
+        e = consider(t);
+      }
+  }
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  if (e != cudaSuccess) return cuda_fail(e, "rt_trace_autotune");
+  scene->tune = best;
+  if (out) {
+    out->launch_shape = (uint32_t)best.variant;
+    out->refill = (uint32_t)best.refill;
+    out->stack_entries = best.stack ? (uint32_t)best.stack : (scene->d.stack_need > 64u ? 192u : 64u);
+    out->tile_nodes = (uint32_t)best.tile;
+    out->best_ms = best_ms;
+  }
+  return RT_OK;
+}
+
+rt_status rt_scene_get_tuning(const rt_scene* scene, RtTraceTuning* out) {
+  if (!scene || !out) {
+    set_error("rt_scene_get_tuning: null argument");
+    return RT_EINVAL;
+  }
+  out->launch_shape = (uint32_t)scene->tune.variant;
+  out->refill = (uint32_t)scene->tune.refill;
+  out->stack_entries = scene->tune.stack ? (uint32_t)scene->tune.stack : (scene->d.stack_need > 64u ? 192u : 64u);
+  out->tile_nodes = (uint32_t)scene->tune.tile;
+  out->best_ms = 0.0f;
+  return RT_OK;
+}
+
+rt_status rt_scene_set_tuning(rt_scene* scene, const RtTraceTuning* in) {
+  if (!scene || !in) {
+    set_error("rt_scene_set_tuning: null argument");
+    return RT_EINVAL;
+  }
+  TraceTuning t = default_tuning();
+  t.variant = (int)in->launch_shape;
+  t.refill = (int)in->refill;
+  t.stack = (int)in->stack_entries;
+  t.tile = (int)in->tile_nodes;
+  const int need_cap = scene->d.stack_need > 64u ? 192 : 64;
+  if (t.stack == need_cap && t.tile == 0) t.stack = 0;  // the default capacity of the shape
+  if (!tuning_supported(t, scene->d.width, scene->d.stack_need, 0)) {
+    set_error("rt_scene_set_tuning: unsupported launch shape, refill, stack capacity or tile for this scene");
+    return RT_EINVAL;
+  }
+  scene->tune = t;
   return RT_OK;
 }
 
@@ -643,7 +761,8 @@ rt_status rt_trace_host(rt_scene* scene, const RtRay* h_rays, uint32_t n, RtHit*
       if ((e = cudaMemsetAsync(counters[b], 0, 2 * sizeof(uint32_t), tst[b])) != cudaSuccess)
         return cuda_fail(e, "memset");
       RtHit* out = direct ? direct + off : dhits[b];
-      if ((e = launch_trace(scene->d, drays[b], cnt, out, flags, counters[b], tst[b], order)) != cudaSuccess)
+      if ((e = launch_trace_tuned(scene->d, drays[b], cnt, out, flags, counters[b], tst[b],
+                                  (flags & RT_TRACE_MT) ? default_tuning() : scene->tune, nullptr, order)) != cudaSuccess)
         return cuda_fail(e, "rt_trace_host: launch");
       if ((e = cudaEventRecord(trace_done[b], tst[b])) != cudaSuccess) return cuda_fail(e, "event");
       if (direct) continue;

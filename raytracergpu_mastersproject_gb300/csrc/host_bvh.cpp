@@ -921,6 +921,26 @@ bool convert_bvh(const RtBVHNode40* nodes, uint32_t nn, const RtTriangle64* tris
     out.root = 0;
     out.depth = dep[0];
     out.stack_need = need[0] + 1u;
+    // Renumber: the top kTopNodes wide nodes in breadth-first order first (so
+    // a kernel can stage the top levels of the tree as one contiguous range
+    // [root, root + K)), the rest in their left-first preorder.
+    {
+      const size_t top = std::min<size_t>(kTopNodes, wn.size());
+      std::vector<uint32_t> perm(wn.size(), NONE);
+      std::vector<uint32_t> bfs{0u};
+      for (size_t h = 0; h < bfs.size() && bfs.size() < top; ++h)
+        for (uint32_t j = 0; j < wn[bfs[h]].count && bfs.size() < top; ++j)
+          if (expandable(wn[bfs[h]].ch[j])) bfs.push_back(dev[wn[bfs[h]].ch[j]]);
+      uint32_t next = 0;
+      for (uint32_t k : bfs) perm[k] = next++;
+      for (size_t k = 0; k < wn.size(); ++k)
+        if (perm[k] == NONE) perm[k] = next++;
+      std::vector<Wide> wn2(wn.size());
+      for (size_t k = 0; k < wn.size(); ++k) wn2[perm[k]] = wn[k];
+      wn.swap(wn2);
+      for (auto& d : dev)
+        if (d != NONE) d = perm[d];
+    }
     // Quantised child boxes: node origin p = min of the child boxes; per axis a
     // power-of-two step s = 2^e with 255*s >= extent; child bounds rounded
     // outward to multiples of s, so p + q*s encloses every child box.

@@ -39,7 +39,7 @@ struct DJob {
   uint32_t start;
   uint32_t count;
   uint32_t root;
-  uint32_t pad;
+  uint32_t nodes;  // the scene's 4-wide nodes [root, root + nodes) in the arena
 };
 static_assert(sizeof(DJob) == 32, "job record is 32 bytes");
 
@@ -63,11 +63,37 @@ __device__ __forceinline__ uint32_t find_job(const DJob* __restrict__ jobs, uint
   return lo;
 }
 
+// Jobs whose scenes' top nodes a block can stage (TILE > 0); batches with
+// more jobs run without the tile.
+constexpr uint32_t kTileJobs = 256;
+
+// Node fetch of k_pool_step with a staged tile: the first `count` nodes of the
+// lane's scene, [base, base + count), from shared memory.
+struct PoolTiledNodes {
+  const float4* tile;
+  uint32_t base, count;
+  __device__ __forceinline__ void operator()(const DeviceScene& S, uint32_t node, float4& h, float4& r, float4& qa,
+                                             float4& qb) const {
+    const uint32_t i = node - base;
+    if (i < count) {
+      h = tile[4u * i + 0u];
+      r = tile[4u * i + 1u];
+      qa = tile[4u * i + 2u];
+      qb = tile[4u * i + 3u];
+    } else {
+      dev::GlobalNodes()(S, node, h, r, qa, qb);
+    }
+  }
+};
+
 // k_trace_step over a job table (see trace.cu): each lane keeps (job, local
 // ray index) and its job's root; hits go to the job's own hit array.
 // RING > 0: the top RING stack entries of each lane in shared memory (see
-// dev::RingStack).
-template <bool ANY, int STACK, int THREADS, int MINB, int RING>
+// dev::RingStack).  TILE > 0: each block stages the first TILE nodes of
+// every job's scene -- its top levels, which the builder numbers first in
+// breadth-first order -- in shared memory (plain loads at block start), when
+// the batch has at most kTileJobs jobs.
+template <bool ANY, int STACK, int THREADS, int MINB, int RING, int TILE = 0>
 __global__ void __launch_bounds__(THREADS, MINB)
     k_pool_step(DeviceScene S, const DJob* __restrict__ table, uint32_t* __restrict__ counter, int refill) {
   uint2 stack[STACK];
@@ -87,6 +113,25 @@ __global__ void __launch_bounds__(THREADS, MINB)
   const uint32_t num_jobs = __ldg(reinterpret_cast<const uint32_t*>(table));
   const uint32_t total = __ldg(reinterpret_cast<const uint32_t*>(table) + 1);
   const DJob* jobs = table + 1;
+  using Fetch = typename std::conditional<(TILE > 0), PoolTiledNodes, dev::GlobalNodes>::type;
+  Fetch fetch;
+  [[maybe_unused]] const float4* tile_base = nullptr;
+  [[maybe_unused]] const bool tiled = TILE > 0 && num_jobs <= kTileJobs;
+  if constexpr (TILE > 0) {
+    __shared__ float4 tile[kTileJobs * TILE * 4];
+    if (tiled) {
+      for (uint32_t i = threadIdx.x; i < num_jobs * TILE * 4u; i += THREADS) {
+        const uint32_t j = i / (TILE * 4u), w = i % (TILE * 4u);
+        const uint32_t root = __ldg(&jobs[j].root), nn = __ldg(&jobs[j].nodes);
+        if (root < kSentinel && w / 4u < nn) tile[i] = dev::ldg4(S.inner, 4u * root + w);
+      }
+    }
+    __syncthreads();
+    tile_base = tile;
+    fetch.tile = tile;
+    fetch.base = 0u;
+    fetch.count = 0u;
+  }
   uint32_t job = 0, local = 0xFFFFFFFFu;
   bool exhausted = total == 0;
   const int min_idle = refill < 1 ? 1 : (refill > 32 ? 32 : refill);
@@ -104,7 +149,13 @@ __global__ void __launch_bounds__(THREADS, MINB)
           job = find_job(jobs, num_jobs, g);
           local = g - __ldg(&jobs[job].start);
           const float4* rays = jobs[job].rays;
-          dev::trav_init_ray(s, __ldg(&rays[2u * local]), __ldg(&rays[2u * local + 1u]), __ldg(&jobs[job].root));
+          const uint32_t root = __ldg(&jobs[job].root);
+          dev::trav_init_ray(s, __ldg(&rays[2u * local]), __ldg(&rays[2u * local + 1u]), root);
+          if constexpr (TILE > 0) {
+            fetch.tile = tile_base + 4u * TILE * job;
+            fetch.base = root;
+            fetch.count = tiled && root < kSentinel ? min((uint32_t)TILE, __ldg(&jobs[job].nodes)) : 0u;
+          }
           stk.reset();
           if (s.leaf != 0u) {
             s.node = s.leaf;
@@ -117,7 +168,7 @@ __global__ void __launch_bounds__(THREADS, MINB)
     bool done = false;
     // a node visit, then in the same iteration the leaf it led to
     if (dev::is_inner(s.node)) {
-      if (!dev::visit_wide_stk<STACK>(S, s, stk)) done = true;
+      if (!dev::visit_wide_stk<STACK>(S, s, stk, fetch)) done = true;
     }
     if (!done && dev::is_leaf(s.node)) {
       if (dev::leaf_visit<ANY>(S, s, s.node))
@@ -161,6 +212,64 @@ PoolVariant g_pool_variants[] = {make_pool_variant<128, 10, 16>(), make_pool_var
                                  make_pool_variant<128, 12, 0>(), make_pool_variant<128, 10, 0>(),
                                  make_pool_variant<256, 6, 0>()};
 constexpr int kNumPoolVariants = sizeof(g_pool_variants) / sizeof(g_pool_variants[0]);
+
+// The tuner's further dimensions, on the two 128 x 10 shapes (variant 0 with
+// the 16-entry shared ring, variant 3 with the stack in local memory):
+// traversal stack capacity and the top-of-tree nodes staged per job.
+constexpr int kPoolStacks[] = {48, 64, 96, 192};
+constexpr int kPoolTiles[] = {0, 1, 2};
+template <bool ANY, int STACK, int RING>
+void fill_pool_tuned_row(PoolKernel* row) {
+  row[0] = k_pool_step<ANY, STACK, 128, 10, RING, 0>;
+  row[1] = k_pool_step<ANY, STACK, 128, 10, RING, 1>;
+  row[2] = k_pool_step<ANY, STACK, 128, 10, RING, 2>;
+}
+template <bool ANY, int RING>
+void fill_pool_tuned_shape(PoolKernel (*rows)[3]) {
+  fill_pool_tuned_row<ANY, 48, RING>(rows[0]);
+  fill_pool_tuned_row<ANY, 64, RING>(rows[1]);
+  fill_pool_tuned_row<ANY, 96, RING>(rows[2]);
+  fill_pool_tuned_row<ANY, 192, RING>(rows[3]);
+}
+struct PoolTuned {
+  PoolKernel k[2][2][4][3];  // [shape: variant 0, variant 3][any][stack][tile]
+  int bps[2][2][4][3];
+  PoolTuned() {
+    fill_pool_tuned_shape<false, 16>(k[0][0]);
+    fill_pool_tuned_shape<true, 16>(k[0][1]);
+    fill_pool_tuned_shape<false, 0>(k[1][0]);
+    fill_pool_tuned_shape<true, 0>(k[1][1]);
+    for (auto& a : bps)
+      for (auto& b : a)
+        for (auto& c : b)
+          for (int& d : c) d = -1;
+  }
+};
+PoolTuned g_pool_tuned;
+
+int pool_index(const int* table, int n, int v) {
+  for (int i = 0; i < n; ++i)
+    if (table[i] == v) return i;
+  return -1;
+}
+
+// The kernel of (variant, stack, tile) or null when the pool cannot run it.
+PoolKernel pool_kernel(int variant, int any, int big, int stack, int tile, uint32_t need, int** bps_slot,
+                       int* threads) {
+  if (variant < 0 || variant >= kNumPoolVariants) return nullptr;
+  PoolVariant& v = g_pool_variants[variant];
+  *threads = v.threads;
+  if (stack == 0 && tile == 0) {
+    *bps_slot = &v.bps[any][big];
+    return v.k[any][big];
+  }
+  const int shape = variant == 0 ? 0 : (variant == 3 ? 1 : -1);
+  const int si = stack == 0 ? (big ? 3 : 1) : pool_index(kPoolStacks, 4, stack);
+  const int ti = pool_index(kPoolTiles, 3, tile);
+  if (shape < 0 || si < 0 || ti < 0 || (uint32_t)kPoolStacks[si] < need) return nullptr;
+  *bps_slot = &g_pool_tuned.bps[shape][any][si][ti];
+  return g_pool_tuned.k[shape][any][si][ti];
+}
 
 // First-fit range allocator over [0, capacity) with coalescing frees.
 class RangeAlloc {
@@ -226,7 +335,7 @@ struct LaunchSlot {
   bool used = false;
   // what the graph was captured with
   uint64_t generation = ~0ull;
-  int variant = -1, any = -1, big = -1, refill = -1;
+  int variant = -1, any = -1, big = -1, refill = -1, stack = -1, tile = -1;
 };
 
 struct StreamState {
@@ -252,6 +361,8 @@ struct rt_pool {
   uint32_t max_stack_need = 1;
   int variant = 0;
   int refill = 4;
+  int stack = 0;  // 0: 64 or 192 entries by the pooled scenes' worst case
+  int tile = 0;   // top-of-tree nodes staged per job (variants 0 and 3)
   std::unordered_map<cudaStream_t, rtgb::StreamState*> streams;
 };
 
@@ -330,7 +441,7 @@ rt_status fill_table(rt_pool* P, const RtJob* jobs, uint32_t num_jobs, DJob* hos
     out[j].start = (uint32_t)total;
     out[j].count = J.num_rays;
     out[j].root = P->scenes[J.scene_id].root;
-    out[j].pad = 0;
+    out[j].nodes = (uint32_t)P->scenes[J.scene_id].node_cnt;
     total += J.num_rays;
     if (total > 0x80000000ull) {
       set_error("rt_pool_trace: more than 2^31 rays in one batch");
@@ -346,15 +457,21 @@ rt_status fill_table(rt_pool* P, const RtJob* jobs, uint32_t num_jobs, DJob* hos
 }
 
 // Captures (table upload, queue reset, kernel) into the slot's graph.
-rt_status capture(rt_pool* P, LaunchSlot& sl, uint32_t* counter, int variant, int any, int big, int refill) {
+rt_status capture(rt_pool* P, LaunchSlot& sl, uint32_t* counter, int variant, int any, int big, int refill,
+                  int stack, int tile) {
   if (sl.exec) cudaGraphExecDestroy(sl.exec);
   if (sl.graph) cudaGraphDestroy(sl.graph);
   sl.exec = nullptr;
   sl.graph = nullptr;
-  PoolVariant& v = g_pool_variants[variant];
-  PoolKernel k = v.k[any][big];
+  int* bps_slot = nullptr;
+  int threads = 0;
+  PoolKernel k = pool_kernel(variant, any, big, stack, tile, P->max_stack_need, &bps_slot, &threads);
+  if (!k) {
+    set_error("rt_pool: launch shape, stack capacity or tile not available for this pool");
+    return RT_EINVAL;
+  }
   int bps = 0;
-  if (cudaError_t oe = cached_blocks_per_sm(&v.bps[any][big], k, v.threads, &bps); oe != cudaSuccess)
+  if (cudaError_t oe = cached_blocks_per_sm(bps_slot, k, threads, &bps); oe != cudaSuccess)
     return cuda_err(oe, "rt_pool: occupancy");
   cudaStream_t cs;
   cudaError_t e = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking);
@@ -364,7 +481,7 @@ rt_status capture(rt_pool* P, LaunchSlot& sl, uint32_t* counter, int variant, in
   if (e == cudaSuccess) e = cudaMemsetAsync(counter, 0, 8, cs);
   if (e == cudaSuccess) {
     const uint32_t blocks = (uint32_t)(device_sm_count() * bps);
-    k<<<blocks, v.threads, 0, cs>>>(arena_view(P), sl.dev, counter, refill);
+    k<<<blocks, threads, 0, cs>>>(arena_view(P), sl.dev, counter, refill);
     e = cudaGetLastError();
   }
   cudaGraph_t g = nullptr;
@@ -379,11 +496,13 @@ rt_status capture(rt_pool* P, LaunchSlot& sl, uint32_t* counter, int variant, in
   sl.any = any;
   sl.big = big;
   sl.refill = refill;
+  sl.stack = stack;
+  sl.tile = tile;
   return RT_OK;
 }
 
 rt_status pool_trace_locked(rt_pool* P, const RtJob* jobs, uint32_t num_jobs, uint32_t flags, cudaStream_t st,
-                            int variant, int refill) {
+                            int variant, int refill, int stack, int tile) {
   rt_status status = RT_OK;
   StreamState* ss = stream_state(P, st, &status);
   if (!ss) return status;
@@ -399,8 +518,8 @@ rt_status pool_trace_locked(rt_pool* P, const RtJob* jobs, uint32_t num_jobs, ui
   const int any = (flags & RT_TRACE_ANY) ? 1 : 0;
   const int big = P->max_stack_need > 64u ? 1 : 0;
   if (!sl.exec || sl.generation != P->generation || sl.variant != variant || sl.any != any || sl.big != big ||
-      sl.refill != refill) {
-    if ((status = capture(P, sl, ss->counter, variant, any, big, refill)) != RT_OK) return status;
+      sl.refill != refill || sl.stack != stack || sl.tile != tile) {
+    if ((status = capture(P, sl, ss->counter, variant, any, big, refill, stack, tile)) != RT_OK) return status;
   }
   cudaError_t e = cudaGraphLaunch(sl.exec, st);
   if (e == cudaSuccess) e = cudaEventRecord(sl.done, st);
@@ -652,6 +771,8 @@ rt_status rt_pool_get_info(const rt_pool* Pc, RtPoolInfo* out) {
   out->num_triangles = (uint32_t)tris;
   out->tuned_variant = (uint32_t)P->variant;
   out->tuned_refill = P->refill;
+  out->tuned_stack = P->stack ? (uint32_t)P->stack : (P->max_stack_need > 64u ? 192u : 64u);
+  out->tuned_tile = (uint32_t)P->tile;
   return RT_OK;
 }
 
@@ -662,7 +783,11 @@ rt_status rt_pool_trace(rt_pool* P, const RtJob* jobs, uint32_t num_jobs, uint32
     return RT_EINVAL;
   }
   std::lock_guard<std::mutex> lk(P->mu);
-  return pool_trace_locked(P, jobs, num_jobs, flags, reinterpret_cast<cudaStream_t>(stream), P->variant, P->refill);
+  // a pool that grew a deeper scene since tuning falls back to the default capacity
+  int stack = P->stack, tile = P->tile;
+  if (stack && (uint32_t)stack < P->max_stack_need) stack = 0, tile = 0;
+  return pool_trace_locked(P, jobs, num_jobs, flags, reinterpret_cast<cudaStream_t>(stream), P->variant, P->refill,
+                           stack, tile);
 }
 
 rt_status rt_pool_autotune(rt_pool* P, const RtJob* jobs, uint32_t num_jobs, uint32_t flags, void* stream,
@@ -680,33 +805,71 @@ rt_status rt_pool_autotune(rt_pool* P, const RtJob* jobs, uint32_t num_jobs, uin
   cudaEventCreate(&a);
   cudaEventCreate(&b);
   float best = 3.4e38f;
-  int bv = P->variant, br = P->refill;
+  int bv = P->variant, br = P->refill, bs = 0, bt = 0;
   rt_status status = RT_OK;
+  auto time_one = [&](int v, int r, int sc, int tl) -> rt_status {
+    // warm-up: captures the graphs of both launch slots outside the timing
+    rt_status rs = pool_trace_locked(P, jobs, num_jobs, flags, st, v, r, sc, tl);
+    if (rs == RT_OK) rs = pool_trace_locked(P, jobs, num_jobs, flags, st, v, r, sc, tl);
+    if (rs != RT_OK) return rs;
+    cudaEventRecord(a, st);
+    for (uint32_t k = 0; k < repeats && rs == RT_OK; ++k) rs = pool_trace_locked(P, jobs, num_jobs, flags, st, v, r, sc, tl);
+    cudaEventRecord(b, st);
+    if (rs != RT_OK) return rs;
+    if (cudaEventSynchronize(b) != cudaSuccess) return cuda_err(cudaGetLastError(), "rt_pool_autotune");
+    float ms = 0.0f;
+    cudaEventElapsedTime(&ms, a, b);
+    if (ms < best) {
+      best = ms;
+      bv = v;
+      br = r;
+      bs = sc;
+      bt = tl;
+    }
+    return RT_OK;
+  };
+  // 1. launch shape x refill threshold
   for (int v = 0; v < kNumPoolVariants && status == RT_OK; ++v)
     for (int r : refills) {
-      // warm-up: captures the graphs of both launch slots outside the timing
-      if ((status = pool_trace_locked(P, jobs, num_jobs, flags, st, v, r)) != RT_OK) break;
-      if ((status = pool_trace_locked(P, jobs, num_jobs, flags, st, v, r)) != RT_OK) break;
-      cudaEventRecord(a, st);
-      for (uint32_t k = 0; k < repeats && status == RT_OK; ++k) status = pool_trace_locked(P, jobs, num_jobs, flags, st, v, r);
-      cudaEventRecord(b, st);
-      if (cudaEventSynchronize(b) != cudaSuccess) {
-        status = cuda_err(cudaGetLastError(), "rt_pool_autotune");
-        break;
-      }
-      float ms = 0.0f;
-      cudaEventElapsedTime(&ms, a, b);
-      if (ms < best) {
-        best = ms;
-        bv = v;
-        br = r;
-      }
+      if ((status = time_one(v, r, 0, 0)) != RT_OK) break;
     }
+  // 2. on the 128 x 10 shapes: stack capacity x top-of-tree tile per job
+  if (status == RT_OK && (bv == 0 || bv == 3)) {
+    const int v = bv, r = br;
+    for (int sc : kPoolStacks)
+      for (int tl : kPoolTiles) {
+        if (status != RT_OK || (uint32_t)sc < P->max_stack_need) continue;
+        status = time_one(v, r, sc, tl);
+      }
+  }
   cudaEventDestroy(a);
   cudaEventDestroy(b);
   if (status != RT_OK) return status;
   P->variant = bv;
   P->refill = br;
+  P->stack = bs;
+  P->tile = bt;
+  return RT_OK;
+}
+
+rt_status rt_pool_set_tuning(rt_pool* P, uint32_t variant, int32_t refill, uint32_t stack_entries,
+                             uint32_t tile_nodes) {
+  if (!P) return RT_EINVAL;
+  std::lock_guard<std::mutex> lk(P->mu);
+  const int big = P->max_stack_need > 64u ? 1 : 0;
+  int stack = (int)stack_entries, tile = (int)tile_nodes;
+  if (stack == (big ? 192 : 64) && tile == 0) stack = 0;  // the shape's default capacity
+  int* slot = nullptr;
+  int threads = 0;
+  if (refill < 0 || refill > 32 || !pool_kernel((int)variant, 0, big, stack, tile, P->max_stack_need, &slot, &threads)) {
+    set_error("rt_pool_set_tuning: unknown launch shape, refill, stack capacity below the pool's need, or a tile on "
+              "a shape without one");
+    return RT_EINVAL;
+  }
+  P->variant = (int)variant;
+  P->refill = refill;
+  P->stack = stack;
+  P->tile = tile;
   return RT_OK;
 }
 

@@ -82,6 +82,10 @@ constexpr uint32_t kDefaultWidth = 4;
 // Largest quantisation step exponent of a 4-wide node: the kernels scale by
 // 2^(e+15) / d with |1/d| <= 2^64, which must stay below 2^128.
 constexpr int kMaxWideExp = 48;
+// The first kTopNodes 4-wide nodes of a tree are its top levels in
+// breadth-first order (the rest follow in preorder), so that the kernels can
+// stage the top of the tree in shared memory as one contiguous range.
+constexpr uint32_t kTopNodes = 64;
 
 struct DeviceScene {
   const void* inner = nullptr;     // float4[4 * n_inner]
@@ -173,10 +177,21 @@ struct TraceTuning {
   int variant = 0;
   int refill = 20;
   int grid_scale = 100;
+  // Default launch shape only (variant kTunedVariant): traversal stack
+  // capacity per lane (0: 64 or 192 by the scene's worst-case need) and the
+  // number of top-of-tree nodes staged in shared memory per block (0: none).
+  int stack = 0;
+  int tile = 0;
 };
+constexpr int kTunedVariant = 6;
+constexpr int kTunedStacks[] = {48, 64, 96, 192};
+constexpr int kTunedTiles[] = {0, 16, 64};
 TraceTuning default_tuning();
 int num_trace_variants();
 void trace_variant_shape(int v, int* threads, int* minb);
+// Whether the tuning can run a scene whose traversal needs `stack_need`
+// entries with `flags` (RT_TRACE_*), and with what stack capacity.
+bool tuning_supported(const TraceTuning& t, uint32_t width, uint32_t stack_need, uint32_t flags);
 cudaError_t launch_trace_tuned(const DeviceScene& s, const RtRay* rays, uint32_t n, RtHit* hits, uint32_t flags,
                                uint32_t* counter, void* stream, const TraceTuning& tune,
                                unsigned long long* stats, const uint32_t* order);

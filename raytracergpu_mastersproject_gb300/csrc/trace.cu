@@ -119,7 +119,12 @@ __global__ void __launch_bounds__(THREADS, MINB)
 //
 // RING > 0 keeps the top RING stack entries of each lane in shared memory
 // (RING * THREADS * 8 bytes per block), the rest in local memory.
-template <bool ANY, int STACK, int THREADS, int MINB, bool STATS, bool RAW = false, int RING = 0, bool MT = false>
+//
+// TILE > 0 stages the tree's first TILE nodes -- its top levels, numbered
+// first in breadth-first order -- in shared memory per block (plain loads at
+// block start), and node visits read them from there.
+template <bool ANY, int STACK, int THREADS, int MINB, bool STATS, bool RAW = false, int RING = 0, bool MT = false,
+          int TILE = 0>
 __global__ void __launch_bounds__(THREADS, MINB)
     k_trace_step(DeviceScene S, const float4* __restrict__ rays, uint32_t n, uint2* __restrict__ hits,
                  uint32_t* __restrict__ counter, int refill, unsigned long long* __restrict__ stats,
@@ -135,6 +140,17 @@ __global__ void __launch_bounds__(THREADS, MINB)
     stk.lo = 0;
   } else {
     stk.a = stack;
+  }
+  using Fetch = typename std::conditional<(TILE > 0), dev::TiledNodes<(TILE > 0 ? TILE : 1)>, dev::GlobalNodes>::type;
+  Fetch fetch;
+  if constexpr (TILE > 0) {
+    __shared__ float4 tile[4 * TILE];
+    // node indices are below n_inner, so slots at and past it are never read
+    const uint32_t words = 4u * min((uint32_t)TILE, S.n_inner);
+    for (uint32_t i = threadIdx.x; i < words; i += THREADS) tile[i] = dev::ldg4(S.inner, i);
+    __syncthreads();
+    fetch.tile = tile;
+    fetch.base = 0u;
   }
   dev::Trav s;
   const uint32_t lane = threadIdx.x & 31u;
@@ -169,7 +185,7 @@ __global__ void __launch_bounds__(THREADS, MINB)
     // a node visit, then in the same iteration the leaf it led to (the warp
     // runs the leaf code in nearly every iteration for some lane anyway)
     if (dev::is_inner(s.node)) {
-      if (!dev::visit_wide_stk<STACK>(S, s, stk)) done = true;
+      if (!dev::visit_wide_stk<STACK>(S, s, stk, fetch)) done = true;
     }
     if (!done && dev::is_leaf(s.node)) {
       if (dev::leaf_visit<ANY, MT>(S, s, s.node))
@@ -288,6 +304,40 @@ MtKernels g_mt = {{{{k_trace<false, 64, 128, 10, 2, false, true>, k_trace<false,
                      k_trace_step<true, 192, 128, 10, false, false, 16, true>}}},
                   {{{-1, -1}, {-1, -1}}, {{-1, -1}, {-1, -1}}}};
 
+// The default launch shape (128 threads, 10 blocks per SM, 16-entry shared
+// ring) at every tuned stack capacity and staging tile (closest and any hit):
+// [any][kTunedStacks index][kTunedTiles index].
+template <bool ANY, int STACK>
+void fill_tuned_row(TraceKernel* row) {
+  row[0] = k_trace_step<ANY, STACK, 128, 10, false, false, 16, false, 0>;
+  row[1] = k_trace_step<ANY, STACK, 128, 10, false, false, 16, false, 16>;
+  row[2] = k_trace_step<ANY, STACK, 128, 10, false, false, 16, false, 64>;
+}
+struct TunedKernels {
+  TraceKernel k[2][4][3];
+  int bps[2][4][3];
+  TunedKernels() {
+    fill_tuned_row<false, 48>(k[0][0]);
+    fill_tuned_row<false, 64>(k[0][1]);
+    fill_tuned_row<false, 96>(k[0][2]);
+    fill_tuned_row<false, 192>(k[0][3]);
+    fill_tuned_row<true, 48>(k[1][0]);
+    fill_tuned_row<true, 64>(k[1][1]);
+    fill_tuned_row<true, 96>(k[1][2]);
+    fill_tuned_row<true, 192>(k[1][3]);
+    for (auto& a : bps)
+      for (auto& b : a)
+        for (int& c : b) c = -1;
+  }
+};
+TunedKernels g_tuned;
+
+int tuned_index(const int* table, int n, int v) {
+  for (int i = 0; i < n; ++i)
+    if (table[i] == v) return i;
+  return -1;
+}
+
 int env_int(const char* name, int dflt) {
   const char* e = std::getenv(name);
   return e ? std::atoi(e) : dflt;
@@ -307,6 +357,14 @@ TraceTuning default_tuning() {
 }
 
 int num_trace_variants() { return kNumVariants; }
+
+bool tuning_supported(const TraceTuning& t, uint32_t width, uint32_t stack_need, uint32_t flags) {
+  if (t.variant < 0 || t.variant >= kNumVariants || t.refill < 0 || t.refill > 32) return false;
+  if (t.stack == 0 && t.tile == 0) return true;
+  if (t.variant != kTunedVariant || width != 4 || (flags & RT_TRACE_MT)) return false;
+  const int si = t.stack == 0 ? (stack_need > 64u ? 3 : 1) : tuned_index(kTunedStacks, 4, t.stack);
+  return si >= 0 && tuned_index(kTunedTiles, 3, t.tile) >= 0 && (uint32_t)kTunedStacks[si] >= stack_need;
+}
 void trace_variant_shape(int v, int* threads, int* minb) {
   *threads = g_variants[v].threads;
   *minb = g_variants[v].minb;
@@ -326,6 +384,13 @@ cudaError_t launch_trace_tuned(const DeviceScene& S, const RtRay* rays, uint32_t
   TraceKernel k = mt ? g_mt.k[wide][any][big] : v.k[st][wide][any][big];
   const int threads = mt ? 128 : v.threads;
   int* slot = mt ? &g_mt.blocks_per_sm[wide][any][big] : &v.blocks_per_sm[st][wide][any][big];
+  if (!stats && (tune.stack != 0 || tune.tile != 0)) {
+    if (!tuning_supported(tune, S.width, S.stack_need, flags)) return cudaErrorInvalidValue;
+    const int si = tune.stack == 0 ? (big ? 3 : 1) : tuned_index(kTunedStacks, 4, tune.stack);
+    const int ti = tuned_index(kTunedTiles, 3, tune.tile);
+    k = g_tuned.k[any][si][ti];
+    slot = &g_tuned.bps[any][si][ti];
+  }
   int bps = 0;
   if (cudaError_t e = cached_blocks_per_sm(slot, k, threads, &bps); e != cudaSuccess) return e;
   const uint32_t warps_per_block = (uint32_t)threads / 32u;

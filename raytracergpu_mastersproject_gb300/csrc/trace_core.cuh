@@ -400,20 +400,50 @@ __device__ __forceinline__ float qbyte(uint32_t w) {
   return __uint_as_float(__byte_perm(w, 0x3F800000u, 0x7604u | ((uint32_t)I << 4)));
 }
 
+// Where a 4-wide node's four float4 come from: global memory through the
+// read-only path ...
+struct GlobalNodes {
+  __device__ __forceinline__ void operator()(const DeviceScene& S, uint32_t node, float4& h, float4& r, float4& qa,
+                                             float4& qb) const {
+    h = ldg4(S.inner, 4u * node + 0u);
+    r = ldg4(S.inner, 4u * node + 1u);
+    qa = ldg4(S.inner, 4u * node + 2u);
+    qb = ldg4(S.inner, 4u * node + 3u);
+  }
+};
+// ... or, for the K nodes [base, base + K) -- the top levels of a tree, which
+// the builder numbers first in breadth-first order -- a copy staged in shared
+// memory (4 float4 per node from `tile`).
+template <int K>
+struct TiledNodes {
+  const float4* tile;
+  uint32_t base;
+  __device__ __forceinline__ void operator()(const DeviceScene& S, uint32_t node, float4& h, float4& r, float4& qa,
+                                             float4& qb) const {
+    const uint32_t i = node - base;
+    if (i < (uint32_t)K) {
+      h = tile[4u * i + 0u];
+      r = tile[4u * i + 1u];
+      qa = tile[4u * i + 2u];
+      qb = tile[4u * i + 3u];
+    } else {
+      GlobalNodes()(S, node, h, r, qa, qb);
+    }
+  }
+};
+
 // One 4-wide inner node: tests its children, pushes all hit children but the
 // nearest, and moves to the nearest (or pops).  Returns false on stack
 // overflow (s.sp = -1).
-template <int STACK, class Stk>
-__device__ __forceinline__ bool visit_wide_stk(const DeviceScene& S, Trav& s, Stk& stk) {
+template <int STACK, class Stk, class Fetch = GlobalNodes>
+__device__ __forceinline__ bool visit_wide_stk(const DeviceScene& S, Trav& s, Stk& stk, const Fetch& fetch = Fetch()) {
   if (chk(S.check, s.node >= S.n_inner, kChkNode, s.node)) {
     s.sp = -1;  // ends the ray like a stack overflow
     return false;
   }
   s.nvis++;
-  const float4 h = ldg4(S.inner, 4u * s.node + 0u);
-  const float4 r = ldg4(S.inner, 4u * s.node + 1u);
-  const float4 qa = ldg4(S.inner, 4u * s.node + 2u);
-  const float4 qb = ldg4(S.inner, 4u * s.node + 3u);
+  float4 h, r, qa, qb;
+  fetch(S, s.node, h, r, qa, qb);
   const uint32_t meta = fbits(h.w);
   const float ax = __uint_as_float((meta & 0xFFu) << 23) * s.ix;
   const float ay = __uint_as_float(((meta >> 8) & 0xFFu) << 23) * s.iy;

@@ -94,3 +94,40 @@ def test_pool_budget_and_empty_jobs(rt, cuda):
         pool.trace([])
         with pytest.raises(rt.RtError):
             pool.trace([(999, d_rays, d_hits)])
+
+
+def test_pool_every_tuning_same_hits(rt, cuda):
+    """Every stack capacity and top-of-tree tile the pool tuner searches (on
+    the two 128 x 10 launch shapes) returns exactly the hits of each scene
+    traced alone; the tuner reports what it chose; settings the pool cannot
+    run are refused.  Also with more jobs than a block can stage (no tile)."""
+    data = soups(rt, 43, 40, hi=30_000)
+    ref = [alone(rt, cuda, t, r) for t, r in data]
+    with rt.Pool() as pool:
+        ids = [pool.add_scene(t) for t, _ in data]
+        need = pool.info().stack_need
+        for variant in (0, 3):
+            for stack in (48, 64, 96, 192):
+                for tile in (0, 1, 2):
+                    if stack < need:
+                        with pytest.raises(rt.RtError):
+                            pool.set_tuning(variant, 4, stack, tile)
+                        continue
+                    pool.set_tuning(variant, 4, stack, tile)
+                    info = pool.info()
+                    assert (info.tuned_variant, info.tuned_stack, info.tuned_tile) == (variant, stack, tile)
+                    got = run_pool(rt, cuda, pool, ids, data)
+                    for g, want in zip(got, ref):
+                        assert np.array_equal(g.view(np.uint64), want.view(np.uint64)), (variant, stack, tile)
+        with pytest.raises(rt.RtError):
+            pool.set_tuning(1, 4, 64, 1)  # tiles only on the 128 x 10 shapes
+        run_pool(rt, cuda, pool, ids, data, autotune=True)
+        info = pool.info()
+        assert info.tuned_stack >= need and info.tuned_tile in (0, 1, 2)
+        # 300 jobs (above the 256 a block stages): the tile is skipped, hits unchanged
+        if info.tuned_variant in (0, 3):
+            pool.set_tuning(info.tuned_variant, 4, 64 if need <= 64 else 192, 2)
+        many = [(ids[i % len(ids)], data[i % len(data)]) for i in range(300)]
+        got = run_pool(rt, cuda, pool, [m[0] for m in many], [m[1] for m in many])
+        for k, g in enumerate(got):
+            assert np.array_equal(g.view(np.uint64), ref[k % len(ref)].view(np.uint64))

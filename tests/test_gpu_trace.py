@@ -534,3 +534,41 @@ def test_mt_mode_rejected_where_unsupported(rt, cuda):
         c = (C.c_uint64 * 2)()
         st = rt.lib().rt_trace_count(sc.handle, d_rays.data_ptr(), 1024, d_hits.data_ptr(), rt.TRACE_MT, None, c)
         assert rt.STATUS[st] == "RT_EINVAL"
+
+
+def test_autotune_and_every_tuning_same_hits(rt, orc, cuda):
+    """rt_trace_autotune picks a launch (shape, refill, stack capacity, staged
+    top-of-tree tile) on the caller's batch; every tuning gives the same hits,
+    bit for bit, and settings a scene cannot run are refused."""
+    tris = rt.gen_soup(31, 0, 200_000, 1.0, 0.002)
+    rays = rt.gen_rays(31, 0, 400_000, 1.0, 1e-4, float("inf"))
+    with rt.Scene(tris) as sc:
+        base = dev_trace(rt, cuda, sc, rays)
+        base_any = dev_trace(rt, cuda, sc, rays, any_hit=True)
+        d_rays = cuda.from_numpy(rays.view(np.uint8)).cuda()
+        d_hits = cuda.empty(len(rays) * 8, dtype=cuda.uint8, device="cuda")
+        t = sc.autotune(d_rays, d_hits, sort=True, repeats=1)
+        assert t.best_ms > 0 and t.stack_entries >= sc.info().stack_need
+        got = sc.tuning()
+        assert (got.launch_shape, got.refill, got.stack_entries, got.tile_nodes) == \
+               (t.launch_shape, t.refill, t.stack_entries, t.tile_nodes)
+        assert np.array_equal(dev_trace(rt, cuda, sc, rays, sort=True).view(np.uint64), base.view(np.uint64))
+        need = sc.info().stack_need
+        for stack in (48, 64, 96, 192):
+            for tile in (0, 16, 64):
+                if stack < need:
+                    with pytest.raises(rt.RtError):
+                        sc.set_tuning(rt.TraceTuning(6, 5, stack, tile, 0.0))
+                    continue
+                sc.set_tuning(rt.TraceTuning(6, 5, stack, tile, 0.0))
+                assert np.array_equal(dev_trace(rt, cuda, sc, rays).view(np.uint64), base.view(np.uint64)), (stack, tile)
+                assert np.array_equal(dev_trace(rt, cuda, sc, rays, any_hit=True).view(np.uint64),
+                                      base_any.view(np.uint64)), (stack, tile)
+        host = sc.trace_host(rays)
+        assert np.array_equal(host.view(np.uint64), base.view(np.uint64))
+        with pytest.raises(rt.RtError):
+            sc.set_tuning(rt.TraceTuning(6, 5, 8, 0, 0.0))    # below the tree's worst case
+        with pytest.raises(rt.RtError):
+            sc.set_tuning(rt.TraceTuning(3, 5, 64, 16, 0.0))  # tiles only on the default shape
+    ref, _ = orc.trace(orc.Scene(tris, orc.build_bvh(tris, mode=0)[0]), rays[:50_000], canonical=True)
+    assert_parity(orc, tris, rays[:50_000], ref, base[:50_000])
