@@ -371,7 +371,8 @@ rt_status rt_pool_get_info(const rt_pool* pool, RtPoolInfo* out_info);
  * identical to rt_trace on each scene alone. */
 rt_status rt_pool_trace(rt_pool* pool, const RtJob* jobs, uint32_t num_jobs, uint32_t flags, void* stream);
 /* Times the jobs under every launch shape (threads per block, register cap)
- * and refill threshold, then, on the two shapes of 128 threads x 10 blocks,
+ * and refill threshold, then, on the two shapes of 128 threads x 10 blocks
+ * with four node visits per iteration (variants 5 and 6),
  * every traversal stack capacity (48, 64, 96, 192 entries, at least the pooled
  * scenes' worst case) and top-of-tree tile (0, 1 or 2 nodes of each job's
  * scene staged in shared memory per block, for batches of up to 256 jobs),
@@ -381,13 +382,15 @@ rt_status rt_pool_autotune(rt_pool* pool, const RtJob* jobs, uint32_t num_jobs, 
                            uint32_t repeats);
 /* Sets the launch rt_pool_trace uses (what rt_pool_autotune would choose):
  * launch shape, refill threshold, stack capacity (0: 64 or 192 by the pooled
- * scenes' worst case) and top-of-tree tile per job (0, 1 or 2; variants 0
- * and 3 only).  RT_EINVAL for a combination the pool cannot run. */
+ * scenes' worst case) and top-of-tree tile per job (0, 1 or 2; variants 5
+ * and 6 only).  RT_EINVAL for a combination the pool cannot run. */
 rt_status rt_pool_set_tuning(rt_pool* pool, uint32_t variant, int32_t refill, uint32_t stack_entries,
                              uint32_t tile_nodes);
 /* Launch shape of a variant: threads per block, minimum resident blocks per
  * SM (the register cap), and the traversal-stack entries kept in shared
- * memory per lane (0: all in local memory).  stack_ring may be NULL. */
+ * memory per lane (0: all in local memory).  stack_ring may be NULL.
+ * Variants 5 (the default) and 6 have the shapes of 0 and 3 and make up to
+ * four node visits per loop iteration. */
 rt_status rt_pool_describe_variant(uint32_t variant, uint32_t* threads, uint32_t* min_blocks,
                                    uint32_t* stack_ring);
 

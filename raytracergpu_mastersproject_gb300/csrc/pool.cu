@@ -93,7 +93,9 @@ struct PoolTiledNodes {
 // every job's scene -- its top levels, which the builder numbers first in
 // breadth-first order -- in shared memory (plain loads at block start), when
 // the batch has at most kTileJobs jobs.
-template <bool ANY, int STACK, int THREADS, int MINB, int RING, int TILE = 0>
+// VISITS > 1: up to VISITS node visits per iteration before the leaf step
+// (see k_trace_step).
+template <bool ANY, int STACK, int THREADS, int MINB, int RING, int TILE = 0, int VISITS = 1>
 __global__ void __launch_bounds__(THREADS, MINB)
     k_pool_step(DeviceScene S, const DJob* __restrict__ table, uint32_t* __restrict__ counter, int refill) {
   uint2 stack[STACK];
@@ -170,6 +172,12 @@ __global__ void __launch_bounds__(THREADS, MINB)
     if (dev::is_inner(s.node)) {
       if (!dev::visit_wide_stk<STACK>(S, s, stk, fetch)) done = true;
     }
+#pragma unroll
+    for (int v = 1; v < VISITS; ++v) {
+      if (!done && dev::is_inner(s.node)) {
+        if (!dev::visit_wide_stk<STACK>(S, s, stk, fetch)) done = true;
+      }
+    }
     if (!done && dev::is_leaf(s.node)) {
       if (dev::leaf_visit<ANY>(S, s, s.node))
         done = true;
@@ -199,30 +207,34 @@ struct PoolVariant {
   int bps[2][2];
 };
 
-template <int T, int M, int R>
+template <int T, int M, int R, int V = 1>
 PoolVariant make_pool_variant() {
-  PoolVariant v{T, M, R, {{k_pool_step<false, 64, T, M, R>, k_pool_step<false, 192, T, M, R>},
-                          {k_pool_step<true, 64, T, M, R>, k_pool_step<true, 192, T, M, R>}},
+  PoolVariant v{T, M, R, {{k_pool_step<false, 64, T, M, R, 0, V>, k_pool_step<false, 192, T, M, R, 0, V>},
+                          {k_pool_step<true, 64, T, M, R, 0, V>, k_pool_step<true, 192, T, M, R, 0, V>}},
                 {{-1, -1}, {-1, -1}}};
   return v;
 }
 
-// Variant 0 is the default before rt_pool_autotune.
+// Variants 5 and 6 are the shapes of 0 and 3 with up to four node visits
+// per iteration; 5 is the default before rt_pool_autotune.
 PoolVariant g_pool_variants[] = {make_pool_variant<128, 10, 16>(), make_pool_variant<256, 5, 16>(),
                                  make_pool_variant<128, 12, 0>(), make_pool_variant<128, 10, 0>(),
-                                 make_pool_variant<256, 6, 0>()};
+                                 make_pool_variant<256, 6, 0>(), make_pool_variant<128, 10, 16, kDefaultVisits>(),
+                                 make_pool_variant<128, 10, 0, kDefaultVisits>()};
+constexpr int kDefaultPoolVariant = 5;
 constexpr int kNumPoolVariants = sizeof(g_pool_variants) / sizeof(g_pool_variants[0]);
 
-// The tuner's further dimensions, on the two 128 x 10 shapes (variant 0 with
-// the 16-entry shared ring, variant 3 with the stack in local memory):
-// traversal stack capacity and the top-of-tree nodes staged per job.
+// The tuner's further dimensions, on the two 128 x 10 shapes with four node
+// visits per iteration (variant 5 with the 16-entry shared ring, variant 6
+// with the stack in local memory): traversal stack capacity and the
+// top-of-tree nodes staged per job.
 constexpr int kPoolStacks[] = {48, 64, 96, 192};
 constexpr int kPoolTiles[] = {0, 1, 2};
 template <bool ANY, int STACK, int RING>
 void fill_pool_tuned_row(PoolKernel* row) {
-  row[0] = k_pool_step<ANY, STACK, 128, 10, RING, 0>;
-  row[1] = k_pool_step<ANY, STACK, 128, 10, RING, 1>;
-  row[2] = k_pool_step<ANY, STACK, 128, 10, RING, 2>;
+  row[0] = k_pool_step<ANY, STACK, 128, 10, RING, 0, kDefaultVisits>;
+  row[1] = k_pool_step<ANY, STACK, 128, 10, RING, 1, kDefaultVisits>;
+  row[2] = k_pool_step<ANY, STACK, 128, 10, RING, 2, kDefaultVisits>;
 }
 template <bool ANY, int RING>
 void fill_pool_tuned_shape(PoolKernel (*rows)[3]) {
@@ -232,7 +244,7 @@ void fill_pool_tuned_shape(PoolKernel (*rows)[3]) {
   fill_pool_tuned_row<ANY, 192, RING>(rows[3]);
 }
 struct PoolTuned {
-  PoolKernel k[2][2][4][3];  // [shape: variant 0, variant 3][any][stack][tile]
+  PoolKernel k[2][2][4][3];  // [shape: variant 5, variant 6][any][stack][tile]
   int bps[2][2][4][3];
   PoolTuned() {
     fill_pool_tuned_shape<false, 16>(k[0][0]);
@@ -263,7 +275,7 @@ PoolKernel pool_kernel(int variant, int any, int big, int stack, int tile, uint3
     *bps_slot = &v.bps[any][big];
     return v.k[any][big];
   }
-  const int shape = variant == 0 ? 0 : (variant == 3 ? 1 : -1);
+  const int shape = variant == 5 ? 0 : (variant == 6 ? 1 : -1);
   const int si = stack == 0 ? (big ? 3 : 1) : pool_index(kPoolStacks, 4, stack);
   const int ti = pool_index(kPoolTiles, 3, tile);
   if (shape < 0 || si < 0 || ti < 0 || (uint32_t)kPoolStacks[si] < need) return nullptr;
@@ -359,7 +371,7 @@ struct rt_pool {
   uint64_t generation = 0;  // bumps whenever the arena arrays move
   std::vector<rtgb::PoolScene> scenes;
   uint32_t max_stack_need = 1;
-  int variant = 0;
+  int variant = rtgb::kDefaultPoolVariant;
   int refill = 4;
   int stack = 0;  // 0: 64 or 192 entries by the pooled scenes' worst case
   int tile = 0;   // top-of-tree nodes staged per job (variants 0 and 3)
@@ -833,8 +845,8 @@ rt_status rt_pool_autotune(rt_pool* P, const RtJob* jobs, uint32_t num_jobs, uin
     for (int r : refills) {
       if ((status = time_one(v, r, 0, 0)) != RT_OK) break;
     }
-  // 2. on the 128 x 10 shapes: stack capacity x top-of-tree tile per job
-  if (status == RT_OK && (bv == 0 || bv == 3)) {
+  // 2. on the 128 x 10 four-visit shapes: stack capacity x top-of-tree tile per job
+  if (status == RT_OK && (bv == 5 || bv == 6)) {
     const int v = bv, r = br;
     for (int sc : kPoolStacks)
       for (int tl : kPoolTiles) {

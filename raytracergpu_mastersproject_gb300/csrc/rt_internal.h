@@ -183,7 +183,8 @@ struct TraceTuning {
   int stack = 0;
   int tile = 0;
 };
-constexpr int kTunedVariant = 6;
+constexpr int kTunedVariant = 12;  // the default launch shape (see trace.cu)
+constexpr int kDefaultVisits = 4;  // node visits per iteration of the default shape
 constexpr int kTunedStacks[] = {48, 64, 96, 192};
 constexpr int kTunedTiles[] = {0, 16, 64};
 TraceTuning default_tuning();

@@ -123,8 +123,13 @@ __global__ void __launch_bounds__(THREADS, MINB)
 // TILE > 0 stages the tree's first TILE nodes -- its top levels, numbered
 // first in breadth-first order -- in shared memory per block (plain loads at
 // block start), and node visits read them from there.
+//
+// VISITS = 2 makes up to two node visits per iteration (the second for lanes
+// still at an inner node) before the leaf step: half the iterations, so the
+// leaf code, which some lane needs in nearly every iteration, and the loop's
+// own work run about half as often.
 template <bool ANY, int STACK, int THREADS, int MINB, bool STATS, bool RAW = false, int RING = 0, bool MT = false,
-          int TILE = 0>
+          int TILE = 0, int VISITS = 1>
 __global__ void __launch_bounds__(THREADS, MINB)
     k_trace_step(DeviceScene S, const float4* __restrict__ rays, uint32_t n, uint2* __restrict__ hits,
                  uint32_t* __restrict__ counter, int refill, unsigned long long* __restrict__ stats,
@@ -186,6 +191,12 @@ __global__ void __launch_bounds__(THREADS, MINB)
     // runs the leaf code in nearly every iteration for some lane anyway)
     if (dev::is_inner(s.node)) {
       if (!dev::visit_wide_stk<STACK>(S, s, stk, fetch)) done = true;
+    }
+#pragma unroll
+    for (int v = 1; v < VISITS; ++v) {
+      if (!done && dev::is_inner(s.node)) {
+        if (!dev::visit_wide_stk<STACK>(S, s, stk, fetch)) done = true;
+      }
     }
     if (!done && dev::is_leaf(s.node)) {
       if (dev::leaf_visit<ANY, MT>(S, s, s.node))
@@ -251,23 +262,23 @@ void fill_variant(Variant& v) {
   v.k[ST][1][1][1] = k_trace<true, 192, T, M, 4, ST>;
 }
 
-template <int T, int M, bool ST, int RING>
+template <int T, int M, bool ST, int RING, int VISITS>
 void fill_step_variant(Variant& v) {
   fill_variant<T, M, ST>(v);  // binary trees keep the while-while loop
-  v.k[ST][1][0][0] = k_trace_step<false, 64, T, M, ST, false, RING>;
-  v.k[ST][1][0][1] = k_trace_step<false, 192, T, M, ST, false, RING>;
-  v.k[ST][1][1][0] = k_trace_step<true, 64, T, M, ST, false, RING>;
-  v.k[ST][1][1][1] = k_trace_step<true, 192, T, M, ST, false, RING>;
+  v.k[ST][1][0][0] = k_trace_step<false, 64, T, M, ST, false, RING, false, 0, VISITS>;
+  v.k[ST][1][0][1] = k_trace_step<false, 192, T, M, ST, false, RING, false, 0, VISITS>;
+  v.k[ST][1][1][0] = k_trace_step<true, 64, T, M, ST, false, RING, false, 0, VISITS>;
+  v.k[ST][1][1][1] = k_trace_step<true, 192, T, M, ST, false, RING, false, 0, VISITS>;
 }
 
-template <int T, int M, bool STEP, int RING = 0>
+template <int T, int M, bool STEP, int RING = 0, int VISITS = 1>
 Variant make_variant() {
   Variant v;
   v.threads = T;
   v.minb = M;
   if constexpr (STEP) {
-    fill_step_variant<T, M, false, RING>(v);
-    fill_step_variant<T, M, true, RING>(v);
+    fill_step_variant<T, M, false, RING, VISITS>(v);
+    fill_step_variant<T, M, true, RING, VISITS>(v);
   } else {
     fill_variant<T, M, false>(v);
     fill_variant<T, M, true>(v);
@@ -281,12 +292,18 @@ Variant make_variant() {
 
 // Launch shapes (RT_TRACE_VARIANT selects one; RT_TRACE_REFILL sets the refill
 // threshold): 0-2 while-while loop at 12 / 10 / 1 blocks per SM, 3-5 step
-// loop with the stack in local memory, 6 (default) step loop at 10 blocks of
-// 128 threads with a 16-entry shared ring, 7 the same as 5 blocks of 256.
+// loop with the stack in local memory, 6 step loop at 10 blocks of 128
+// threads with a 16-entry shared ring, 7 the same as 5 blocks of 256; 8-9,
+// 10-11 and 12-13 are the shapes of 6 and 7 with up to two, three and four
+// node visits per iteration.  12 is the default (config 3: 11.78 ms per step
+// against 13.24 with one visit; six and eight visits were slower again).
 // Binary trees always use the while-while loop of the chosen shape.
 Variant g_variants[] = {make_variant<128, 12, false>(), make_variant<128, 10, false>(), make_variant<128, 1, false>(),
                         make_variant<128, 12, true>(),  make_variant<128, 10, true>(),  make_variant<128, 1, true>(),
-                        make_variant<128, 10, true, 16>(), make_variant<256, 5, true, 16>()};
+                        make_variant<128, 10, true, 16>(), make_variant<256, 5, true, 16>(),
+                        make_variant<128, 10, true, 16, 2>(), make_variant<256, 5, true, 16, 2>(),
+                        make_variant<128, 10, true, 16, 3>(), make_variant<256, 5, true, 16, 3>(),
+                        make_variant<128, 10, true, 16, 4>(), make_variant<256, 5, true, 16, 4>()};
 constexpr int kNumVariants = sizeof(g_variants) / sizeof(g_variants[0]);
 
 // RT_TRACE_MT: the Moller-Trumbore leaf test in the default launch shape (the
@@ -298,20 +315,21 @@ struct MtKernels {
 };
 MtKernels g_mt = {{{{k_trace<false, 64, 128, 10, 2, false, true>, k_trace<false, 128, 128, 10, 2, false, true>},
                     {k_trace<true, 64, 128, 10, 2, false, true>, k_trace<true, 128, 128, 10, 2, false, true>}},
-                   {{k_trace_step<false, 64, 128, 10, false, false, 16, true>,
-                     k_trace_step<false, 192, 128, 10, false, false, 16, true>},
-                    {k_trace_step<true, 64, 128, 10, false, false, 16, true>,
-                     k_trace_step<true, 192, 128, 10, false, false, 16, true>}}},
+                   {{k_trace_step<false, 64, 128, 10, false, false, 16, true, 0, kDefaultVisits>,
+                     k_trace_step<false, 192, 128, 10, false, false, 16, true, 0, kDefaultVisits>},
+                    {k_trace_step<true, 64, 128, 10, false, false, 16, true, 0, kDefaultVisits>,
+                     k_trace_step<true, 192, 128, 10, false, false, 16, true, 0, kDefaultVisits>}}},
                   {{{-1, -1}, {-1, -1}}, {{-1, -1}, {-1, -1}}}};
 
 // The default launch shape (128 threads, 10 blocks per SM, 16-entry shared
-// ring) at every tuned stack capacity and staging tile (closest and any hit):
+// ring, four node visits per iteration) at every tuned stack capacity and
+// staging tile (closest and any hit):
 // [any][kTunedStacks index][kTunedTiles index].
 template <bool ANY, int STACK>
 void fill_tuned_row(TraceKernel* row) {
-  row[0] = k_trace_step<ANY, STACK, 128, 10, false, false, 16, false, 0>;
-  row[1] = k_trace_step<ANY, STACK, 128, 10, false, false, 16, false, 16>;
-  row[2] = k_trace_step<ANY, STACK, 128, 10, false, false, 16, false, 64>;
+  row[0] = k_trace_step<ANY, STACK, 128, 10, false, false, 16, false, 0, kDefaultVisits>;
+  row[1] = k_trace_step<ANY, STACK, 128, 10, false, false, 16, false, 16, kDefaultVisits>;
+  row[2] = k_trace_step<ANY, STACK, 128, 10, false, false, 16, false, 64, kDefaultVisits>;
 }
 struct TunedKernels {
   TraceKernel k[2][4][3];
@@ -348,7 +366,7 @@ int env_int(const char* name, int dflt) {
 TraceTuning default_tuning() {
   static TraceTuning t = [] {
     TraceTuning d;
-    d.variant = env_int("RT_TRACE_VARIANT", 6);
+    d.variant = env_int("RT_TRACE_VARIANT", kTunedVariant);
     d.refill = env_int("RT_TRACE_REFILL", 5);
     d.grid_scale = env_int("RT_TRACE_GRID_PCT", 100);
     return d;
@@ -425,12 +443,17 @@ cudaError_t launch_trace_raw(const DeviceScene& S, const float4* rays, uint32_t 
                              unsigned long long* stats, cudaStream_t st) {
   constexpr int T = 128, M = 10, R = 16;  // the default ray-query shape
   const bool big = S.stack_need > 64u;
-  const int k = (big ? 1 : 0) | (stats ? 2 : 0);
-  static int bps[4] = {-1, -1, -1, -1};
-  TraceKernel kern = big ? (stats ? k_trace_step<false, 192, T, M, true, true, R>
-                                  : k_trace_step<false, 192, T, M, false, true, R>)
-                         : (stats ? k_trace_step<false, 64, T, M, true, true, R>
-                                  : k_trace_step<false, 64, T, M, false, true, R>);
+  // node visits per iteration of the bounce queries (RT_TRACE_RAW_VISITS, 1 or 2)
+  // (config 2 extended: 3.44 against 3.51 ms per frame with two)
+  static const int visits = env_int("RT_TRACE_RAW_VISITS", 2) == 1 ? 1 : 2;
+  const int k = (big ? 1 : 0) | (stats ? 2 : 0) | (visits == 2 ? 4 : 0);
+  static int bps[8] = {-1, -1, -1, -1, -1, -1, -1, -1};
+  static const TraceKernel table[8] = {
+      k_trace_step<false, 64, T, M, false, true, R>,         k_trace_step<false, 192, T, M, false, true, R>,
+      k_trace_step<false, 64, T, M, true, true, R>,          k_trace_step<false, 192, T, M, true, true, R>,
+      k_trace_step<false, 64, T, M, false, true, R, false, 0, 2>, k_trace_step<false, 192, T, M, false, true, R, false, 0, 2>,
+      k_trace_step<false, 64, T, M, true, true, R, false, 0, 2>,  k_trace_step<false, 192, T, M, true, true, R, false, 0, 2>};
+  TraceKernel kern = table[k];
   int per_sm = 0;
   if (cudaError_t e = cached_blocks_per_sm(&bps[k], kern, T, &per_sm); e != cudaSuccess) return e;
   uint64_t blocks = (uint64_t)device_sm_count() * (uint64_t)per_sm;

@@ -98,7 +98,7 @@ def test_pool_budget_and_empty_jobs(rt, cuda):
 
 def test_pool_every_tuning_same_hits(rt, cuda):
     """Every stack capacity and top-of-tree tile the pool tuner searches (on
-    the two 128 x 10 launch shapes) returns exactly the hits of each scene
+    the two 128 x 10 four-visit launch shapes) returns exactly the hits of each scene
     traced alone; the tuner reports what it chose; settings the pool cannot
     run are refused.  Also with more jobs than a block can stage (no tile)."""
     data = soups(rt, 43, 40, hi=30_000)
@@ -106,7 +106,7 @@ def test_pool_every_tuning_same_hits(rt, cuda):
     with rt.Pool() as pool:
         ids = [pool.add_scene(t) for t, _ in data]
         need = pool.info().stack_need
-        for variant in (0, 3):
+        for variant in (5, 6):
             for stack in (48, 64, 96, 192):
                 for tile in (0, 1, 2):
                     if stack < need:
@@ -125,7 +125,7 @@ def test_pool_every_tuning_same_hits(rt, cuda):
         info = pool.info()
         assert info.tuned_stack >= need and info.tuned_tile in (0, 1, 2)
         # 300 jobs (above the 256 a block stages): the tile is skipped, hits unchanged
-        if info.tuned_variant in (0, 3):
+        if info.tuned_variant in (5, 6):
             pool.set_tuning(info.tuned_variant, 4, 64 if need <= 64 else 192, 2)
         many = [(ids[i % len(ids)], data[i % len(data)]) for i in range(300)]
         got = run_pool(rt, cuda, pool, [m[0] for m in many], [m[1] for m in many])

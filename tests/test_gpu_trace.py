@@ -558,16 +558,16 @@ def test_autotune_and_every_tuning_same_hits(rt, orc, cuda):
             for tile in (0, 16, 64):
                 if stack < need:
                     with pytest.raises(rt.RtError):
-                        sc.set_tuning(rt.TraceTuning(6, 5, stack, tile, 0.0))
+                        sc.set_tuning(rt.TraceTuning(12, 5, stack, tile, 0.0))
                     continue
-                sc.set_tuning(rt.TraceTuning(6, 5, stack, tile, 0.0))
+                sc.set_tuning(rt.TraceTuning(12, 5, stack, tile, 0.0))
                 assert np.array_equal(dev_trace(rt, cuda, sc, rays).view(np.uint64), base.view(np.uint64)), (stack, tile)
                 assert np.array_equal(dev_trace(rt, cuda, sc, rays, any_hit=True).view(np.uint64),
                                       base_any.view(np.uint64)), (stack, tile)
         host = sc.trace_host(rays)
         assert np.array_equal(host.view(np.uint64), base.view(np.uint64))
         with pytest.raises(rt.RtError):
-            sc.set_tuning(rt.TraceTuning(6, 5, 8, 0, 0.0))    # below the tree's worst case
+            sc.set_tuning(rt.TraceTuning(12, 5, 8, 0, 0.0))    # below the tree's worst case
         with pytest.raises(rt.RtError):
             sc.set_tuning(rt.TraceTuning(3, 5, 64, 16, 0.0))  # tiles only on the default shape
     ref, _ = orc.trace(orc.Scene(tris, orc.build_bvh(tris, mode=0)[0]), rays[:50_000], canonical=True)
