@@ -986,14 +986,14 @@ bool convert_bvh(const RtBVHNode40* nodes, uint32_t nn, const RtTriangle64* tris
         }
         float* o = &out.inner[16 * i];
         o[0] = lo[0]; o[1] = lo[1]; o[2] = lo[2];
-        // exponent bytes hold e + 15 + 127: the kernels read 2^(e+15) directly
-        o[3] = bits_f((uint32_t)(ex[0] + 142) | ((uint32_t)(ex[1] + 142) << 8) | ((uint32_t)(ex[2] + 142) << 16) |
-                      (w.count << 24));
+        // the per-axis scales 2^(e+15) as floats (exact powers of two), which the
+        // kernels multiply by 1/d: x in word 3, y and z in words 14 and 15
+        o[3] = std::ldexp(1.0f, ex[0] + 15);
         for (uint32_t j = 0; j < 4; ++j)
           o[4 + j] = bits_f(j < w.count ? ref_of(w.ch[j], dev) : (kLeafBit | kSphereBit | kSphereMask));
         for (int k = 0; k < 6; ++k) o[8 + k] = bits_f(q[k]);
-        o[14] = 0.0f;
-        o[15] = 0.0f;
+        o[14] = std::ldexp(1.0f, ex[1] + 15);
+        o[15] = std::ldexp(1.0f, ex[2] + 15);
       }
     });
   }

@@ -308,10 +308,10 @@ __device__ __forceinline__ bool trav_run(const DeviceScene& S, Trav& s, uint32_t
 }
 
 // ------------------------------------------------------ 4-wide nodes ----
-// Node (64 B): float4 (p.xyz, meta), uint4 refs, uint4 (qlo_x, qhi_x, qlo_y,
-// qhi_y), uint4 (qlo_z, qhi_z, -, -); meta = exponent bytes (e + 15 + 127 per
-// axis) | child count << 24.  Child i spans p + q*2^e per axis, with q the
-// i-th byte of the matching word.
+// Node (64 B): float4 (p.xyz, 2^(e_x+15)), uint4 refs, uint4 (qlo_x, qhi_x,
+// qlo_y, qhi_y), uint4 (qlo_z, qhi_z, 2^(e_y+15), 2^(e_z+15)) -- the three
+// per-axis scales stored as floats.  Child i spans p + q*2^e per axis, with q
+// the i-th byte of the matching word.
 //
 // A plane's parameter t = (p + q*2^e - o)/d is evaluated as one fma,
 // fma(Q, A, C) with Q = 1 + q*2^-15 (the byte placed in the mantissa under
@@ -444,10 +444,7 @@ __device__ __forceinline__ bool visit_wide_stk(const DeviceScene& S, Trav& s, St
   s.nvis++;
   float4 h, r, qa, qb;
   fetch(S, s.node, h, r, qa, qb);
-  const uint32_t meta = fbits(h.w);
-  const float ax = __uint_as_float((meta & 0xFFu) << 23) * s.ix;
-  const float ay = __uint_as_float(((meta >> 8) & 0xFFu) << 23) * s.iy;
-  const float az = __uint_as_float(((meta >> 16) & 0xFFu) << 23) * s.iz;
+  const float ax = h.w * s.ix, ay = qb.z * s.iy, az = qb.w * s.iz;
   const float bx = (h.x - s.ox) * s.ix, by = (h.y - s.oy) * s.iy, bz = (h.z - s.oz) * s.iz;
   const float cx = bx - ax, cy = by - ay, cz = bz - az;
   const float mx = (fabsf(bx) + fabsf(cx) + fabsf(ax)) * kWideWidenB;
