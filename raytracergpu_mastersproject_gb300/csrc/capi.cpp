@@ -687,7 +687,13 @@ rt_status rt_trace_host(rt_scene* scene, const RtRay* h_rays, uint32_t n, RtHit*
     return v >= 4096 && v <= (1l << 30) ? (uint32_t)v : (1u << 19);
   }();
   RtHit* direct = nullptr;
-  {
+  // RT_HOST_DIRECT_HITS=0 stages the hits in device memory even when h_hits
+  // is page-locked (a measurement knob; read once)
+  static const bool kDirectHits = [] {
+    const char* e = std::getenv("RT_HOST_DIRECT_HITS");
+    return !(e && e[0] == '0');
+  }();
+  if (kDirectHits) {
     cudaPointerAttributes pa;
     if (cudaPointerGetAttributes(&pa, h_hits) == cudaSuccess && pa.type == cudaMemoryTypeHost && pa.devicePointer)
       direct = static_cast<RtHit*>(pa.devicePointer);

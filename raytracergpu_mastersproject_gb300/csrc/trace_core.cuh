@@ -320,11 +320,13 @@ __device__ __forceinline__ bool trav_run(const DeviceScene& S, Trav& s, uint32_t
 // 1/d, p - o, the product, B - A and the fma keep it within
 // 2^-24 (4|B| + 3|C| + 2.02|A|) of the exact value (|t| <= |C| + 1.008|A|).
 // Each axis therefore uses C - M for its near plane and C + M for its far
-// plane, with M = (|B| + |C| + |A|) * 2^-21 -- twice that bound and more, and
-// at most 1/64 of a quantisation step (|A| * 2^-21 = 2^e/|d| * 2^-6) beyond
-// the distance-relative terms.  The near plane of an axis is the low bound
-// when d >= 0 and the high bound otherwise, so no per-axis min/max is needed.
-constexpr float kWideWidenB = 4.76837158203125e-07f;  // 2^-21
+// plane, with M = (|B| + |A|) * 2^-20: since |C| <= (|B| + |A|)(1 + 2^-24) the
+// bound is below 2^-24 (7.01|B| + 5.03|A|), so M is twice the bound and more
+// (the rounding of |B| + |A| and of the fma C -+ M fit in the rest), and at
+// most 1/32 of a quantisation step (|A| * 2^-20 = 2^e/|d| * 2^-5) beyond the
+// distance-relative terms.  The near plane of an axis is the low bound when
+// d >= 0 and the high bound otherwise, so no per-axis min/max is needed.
+constexpr float kWideWiden = 9.5367431640625e-07f;  // 2^-20
 
 // Stack entries are (ref, t_near); an entry that starts beyond the closest
 // hit is dropped when popped, without fetching it.  sp counts entries.
@@ -341,6 +343,13 @@ struct LocalStack {
   uint2* a;
   __device__ __forceinline__ void reset() {}
   __device__ __forceinline__ void push(Trav& s, uint2 e) { a[s.sp++] = e; }
+  // pushes the entries whose flag is set, in argument order (np of them)
+  __device__ __forceinline__ void push3(Trav& s, int np, bool va, uint2 ea, bool vb, uint2 eb, bool vc, uint2 ec) {
+    (void)np;
+    if (va) a[s.sp++] = ea;
+    if (vb) a[s.sp++] = eb;
+    if (vc) a[s.sp++] = ec;
+  }
   __device__ __forceinline__ uint32_t pop(Trav& s) { return pop_wide(s, a); }
 };
 
@@ -364,6 +373,19 @@ struct RingStack {
     }
     ring[(s.sp & (K - 1)) * T] = e;
     ++s.sp;
+  }
+  // pushes the entries whose flag is set, in argument order (np of them):
+  // one check for room in the ring, then the stores
+  __device__ __forceinline__ void push3(Trav& s, int np, bool va, uint2 ea, bool vb, uint2 eb, bool vc, uint2 ec) {
+    while (s.sp + np - lo > K) {
+      spill[lo] = ring[(lo & (K - 1)) * T];
+      ++lo;
+    }
+    int p = s.sp;
+    if (va) ring[(p++ & (K - 1)) * T] = ea;
+    if (vb) ring[(p++ & (K - 1)) * T] = eb;
+    if (vc) ring[(p++ & (K - 1)) * T] = ec;
+    s.sp = p;
   }
   __device__ __forceinline__ uint32_t pop(Trav& s) {
     while (s.sp > 0) {
@@ -447,12 +469,10 @@ __device__ __forceinline__ bool visit_wide_stk(const DeviceScene& S, Trav& s, St
   const float ax = h.w * s.ix, ay = qb.z * s.iy, az = qb.w * s.iz;
   const float bx = (h.x - s.ox) * s.ix, by = (h.y - s.oy) * s.iy, bz = (h.z - s.oz) * s.iz;
   const float cx = bx - ax, cy = by - ay, cz = bz - az;
-  const float mx = (fabsf(bx) + fabsf(cx) + fabsf(ax)) * kWideWidenB;
-  const float my = (fabsf(by) + fabsf(cy) + fabsf(ay)) * kWideWidenB;
-  const float mz = (fabsf(bz) + fabsf(cz) + fabsf(az)) * kWideWidenB;
-  const float bxn = cx - mx, bxf = cx + mx;
-  const float byn = cy - my, byf = cy + my;
-  const float bzn = cz - mz, bzf = cz + mz;
+  const float mx = fabsf(bx) + fabsf(ax), my = fabsf(by) + fabsf(ay), mz = fabsf(bz) + fabsf(az);
+  const float bxn = fmaf(mx, -kWideWiden, cx), bxf = fmaf(mx, kWideWiden, cx);
+  const float byn = fmaf(my, -kWideWiden, cy), byf = fmaf(my, kWideWiden, cy);
+  const float bzn = fmaf(mz, -kWideWiden, cz), bzf = fmaf(mz, kWideWiden, cz);
   // near/far words per axis from the direction's sign; unused child slots
   // hold qlo = 255 > qhi = 0, an empty interval for either sign.
   const uint32_t nx = s.ix >= 0.0f ? fbits(qa.x) : fbits(qa.y), fx = s.ix >= 0.0f ? fbits(qa.y) : fbits(qa.x);
@@ -479,18 +499,19 @@ __device__ __forceinline__ bool visit_wide_stk(const DeviceScene& S, Trav& s, St
   }
   RT_SWAP(t0, r0, t1, r1) RT_SWAP(t2, r2, t3, r3) RT_SWAP(t0, r0, t2, r2)
 #undef RT_SWAP
-  // t0 is the minimum; t2 (the other pair's minimum) is pushed last
-  const int nh = (t0 < inf) + (t1 < inf) + (t2 < inf) + (t3 < inf);
-  if (nh == 0) {
+  // t0 is the minimum (inf: no child hit); t2 (the other pair's minimum) is
+  // pushed last
+  if (!(t0 < inf)) {
     s.node = stk.pop(s);
   } else {
-    if (s.sp + nh - 1 > STACK) {
+    const bool v3 = t3 < inf, v1 = t1 < inf, v2 = t2 < inf;
+    const int np = (int)v3 + (int)v1 + (int)v2;
+    if (s.sp + np > STACK) {
       s.sp = -1;
       return false;
     }
-    if (t3 < inf) stk.push(s, make_uint2(r3, __float_as_uint(t3)));
-    if (t1 < inf) stk.push(s, make_uint2(r1, __float_as_uint(t1)));
-    if (t2 < inf) stk.push(s, make_uint2(r2, __float_as_uint(t2)));
+    stk.push3(s, np, v3, make_uint2(r3, __float_as_uint(t3)), v1, make_uint2(r1, __float_as_uint(t1)), v2,
+              make_uint2(r2, __float_as_uint(t2)));
     s.node = r0;
   }
   return true;
