@@ -676,22 +676,28 @@ rt_status rt_trace_host(rt_scene* scene, const RtRay* h_rays, uint32_t n, RtHit*
   // falling SIMT efficiency, so chunks are few and large: the first is small
   // (its upload is not overlapped) and each next one several times larger.
   //
-  // Hits: when h_hits is page-locked host memory the kernels write them
-  // there directly over the host link (scattered 8-byte stores, overlapped
-  // with tracing), so nothing is downloaded at the end and chunks grow 8x;
-  // otherwise they are staged in device memory and downloaded per chunk on a
-  // third stream, and chunks grow 4x (a smaller last chunk to download).
+  // Hits are staged in device memory and downloaded per chunk on a third
+  // stream; chunks grow 4x, and the plan ends with a small chunk, so that the
+  // one download that overlaps nothing is short.  With RT_HOST_DIRECT_HITS=1
+  // and page-locked h_hits the kernels instead write the hits there directly
+  // over the host link (scattered 8-byte stores, overlapped with tracing) and
+  // chunks grow 8x; on GB300 that measured no faster than staging (config 3:
+  // 12.55-13.03 ms against 12.36-12.55 ms per 16 Mi rays on the same boxes).
   static const uint32_t kFirstChunk = [] {
     const char* e = std::getenv("RT_HOST_FIRST_CHUNK_RAYS");
     const long v = e ? std::atol(e) : 0;
     return v >= 4096 && v <= (1l << 30) ? (uint32_t)v : (1u << 19);
   }();
+  static const uint32_t kLastChunk = [] {
+    const char* e = std::getenv("RT_HOST_LAST_CHUNK_RAYS");
+    if (!e) return 1u << 19;
+    const long v = std::atol(e);
+    return v >= 0 && v <= (1l << 30) ? (uint32_t)v : (1u << 19);
+  }();
   RtHit* direct = nullptr;
-  // RT_HOST_DIRECT_HITS=0 stages the hits in device memory even when h_hits
-  // is page-locked (a measurement knob; read once)
   static const bool kDirectHits = [] {
     const char* e = std::getenv("RT_HOST_DIRECT_HITS");
-    return !(e && e[0] == '0');
+    return e && e[0] == '1';
   }();
   if (kDirectHits) {
     cudaPointerAttributes pa;
@@ -753,6 +759,8 @@ rt_status rt_trace_host(rt_scene* scene, const RtRay* h_rays, uint32_t n, RtHit*
          ++c, off += cnt, size = (uint32_t)std::min<uint64_t>((uint64_t)growth * size, chunk)) {
       const uint32_t b = c & 1u;
       cnt = std::min(size, n - off);
+      // staged: leave exactly kLastChunk rays for the last chunk
+      if (!direct && kLastChunk && n - off > kLastChunk && n - off - cnt < kLastChunk) cnt = n - off - kLastChunk;
       chunks = c + 1;
       if (c >= 2 && (e = cudaStreamWaitEvent(w->copy_in, free_again[b], 0)) != cudaSuccess)
         return cuda_fail(e, "wait");
