@@ -305,12 +305,11 @@ rt_status rt_scene_set_tuning(rt_scene* scene, const RtTraceTuning* tuning);
  *
  * Its scratch is a file-scope device array of RT_NOALLOC_SCRATCH_BYTES that
  * every GPU which loads the library holds until the process exits; the
- * kernel uses its first word, the ray-queue counter.  The first call on a
- * device, with that device current, looks up the array's device address
- * (cudaGetSymbolAddress) and keeps it for the process; make that first call
- * before any stream capture, and do not call across a cudaDeviceReset (the
- * kept address would be stale; rt_trace's per-stream workspaces have the same
- * rule).  All calls share the one array and it keeps the last call's
+ * kernel uses its first word, the ray-queue counter.  Every call looks up
+ * the array's address on the current device (cudaGetSymbolAddress), so no
+ * address is kept across a cudaDeviceReset; the first call on a device loads
+ * the library's device code, so make it before any stream capture.  All calls
+ * share the one array and it keeps the last call's
  * contents (each call zeroes the counter first): calls that overlap on the
  * GPU -- on different streams or from different host threads -- race and
  * must be serialised by the caller.

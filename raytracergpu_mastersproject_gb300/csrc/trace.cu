@@ -15,7 +15,6 @@
 #include <algorithm>
 #include <cstdlib>
 #include <type_traits>
-#include <mutex>
 
 #include "trace_core.cuh"
 
@@ -472,12 +471,6 @@ cudaError_t launch_trace_raw(const DeviceScene& S, const float4* rays, uint32_t 
 // library holds this array until the process exits; all calls share it.
 static __device__ __align__(256) uint32_t g_noalloc_scratch[RT_NOALLOC_SCRATCH_BYTES / sizeof(uint32_t)];
 
-namespace {
-constexpr int kMaxDevices = 64;
-std::mutex g_noalloc_mu;
-uint32_t* g_noalloc_ptr[kMaxDevices] = {};
-}  // namespace
-
 const DeviceScene* scene_device(const rt_scene* scene);
 void set_error(const std::string& msg);
 
@@ -497,31 +490,19 @@ extern "C" rt_status rt_trace_noalloc(rt_scene* scene, const RtRay* d_rays, uint
     return RT_EINVAL;
   }
   if (n == 0) return RT_OK;
-  int dev = 0;
-  cudaError_t e = cudaGetDevice(&dev);
-  if (e != cudaSuccess) {
-    set_error(std::string("rt_trace_noalloc: cudaGetDevice: ") + cudaGetErrorString(e));
-    return RT_ECUDA;
-  }
-  if (dev < 0 || dev >= kMaxDevices) {
-    set_error("rt_trace_noalloc: device ordinal above 63");
-    return RT_EINVAL;
-  }
+  // The host-side name g_noalloc_scratch is not a device address: resolve
+  // the symbol on the current device, every call (no cached address can go
+  // stale when a context is torn down and rebuilt; no allocation either).
   uint32_t* scratch = nullptr;
+  cudaError_t e;
   {
-    // Set-up, once per device, with that device current: the host-side name
-    // g_noalloc_scratch is not a device address, so resolve the symbol.
-    std::lock_guard<std::mutex> lk(g_noalloc_mu);
-    if (!g_noalloc_ptr[dev]) {
-      void* p = nullptr;
-      e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-      if (e != cudaSuccess || !p) {
-        set_error(std::string("rt_trace_noalloc: cudaGetSymbolAddress: ") + cudaGetErrorString(e));
-        return RT_ECUDA;
-      }
-      g_noalloc_ptr[dev] = static_cast<uint32_t*>(p);
+    void* p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess || !p) {
+      set_error(std::string("rt_trace_noalloc: cudaGetSymbolAddress: ") + cudaGetErrorString(e));
+      return RT_ECUDA;
     }
-    scratch = g_noalloc_ptr[dev];
+    scratch = static_cast<uint32_t*>(p);
   }
   cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
   // The array keeps the previous call's contents: the queue counter must
