@@ -131,27 +131,50 @@ __global__ void __launch_bounds__(kT) k_rs_hist(const uint32_t* keys, uint32_t n
   hist[threadIdx.x * tiles + blockIdx.x] = h[threadIdx.x];
 }
 
-// Exclusive scan of `len` counts in place, one block of 1024 threads.
+// Exclusive scan of `len` counts in place, one block of 1024 threads, in
+// chunks of 8192: each thread sums 8 consecutive counts, a warp scan with
+// __shfl_up_sync and a scan of the 32 warp totals give each thread its
+// starting offset, and a running carry links the chunks.  (Loads of
+// consecutive threads stay within the same sectors; a thread-per-stretch
+// serial scan made every load of a warp touch 32 lines.)
 __global__ void __launch_bounds__(1024) k_scan_inplace(uint32_t* a, uint32_t len) {
-  __shared__ uint32_t part[1024];
-  const uint32_t t = threadIdx.x;
-  const uint32_t per = (len + 1023u) / 1024u;
-  const uint32_t b = t * per, e = min(len, b + per);
-  uint32_t sum = 0;
-  for (uint32_t i = b; i < e; ++i) sum += a[i];
-  part[t] = sum;
-  __syncthreads();
-  for (uint32_t off = 1; off < 1024; off <<= 1) {
-    const uint32_t x = t >= off ? part[t - off] : 0u;
+  __shared__ uint32_t warp_sums[32];
+  const uint32_t t = threadIdx.x, lane = t & 31u, w = t >> 5;
+  uint32_t carry = 0;
+  for (uint32_t base = 0; base < len; base += 8192u) {
+    const uint32_t i0 = base + 8u * t;
+    uint32_t v[8], sum = 0;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+      v[k] = i0 + k < len ? a[i0 + k] : 0u;
+      sum += v[k];
+    }
+    uint32_t x = sum;  // inclusive scan over the warp
+#pragma unroll
+    for (uint32_t off = 1; off < 32; off <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, x, off);
+      if (lane >= off) x += y;
+    }
+    if (lane == 31u) warp_sums[w] = x;
     __syncthreads();
-    part[t] += x;
+    if (w == 0) {
+      uint32_t z = warp_sums[lane];
+#pragma unroll
+      for (uint32_t off = 1; off < 32; off <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, z, off);
+        if (lane >= off) z += y;
+      }
+      warp_sums[lane] = z;  // inclusive prefix of the warp totals
+    }
     __syncthreads();
-  }
-  uint32_t run = part[t] - sum;
-  for (uint32_t i = b; i < e; ++i) {
-    const uint32_t v = a[i];
-    a[i] = run;
-    run += v;
+    uint32_t run = carry + (w ? warp_sums[w - 1] : 0u) + x - sum;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+      if (i0 + k < len) a[i0 + k] = run;
+      run += v[k];
+    }
+    carry += warp_sums[31];
+    __syncthreads();  // warp_sums is rewritten by the next chunk
   }
 }
 

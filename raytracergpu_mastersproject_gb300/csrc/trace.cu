@@ -442,16 +442,20 @@ cudaError_t launch_trace_raw(const DeviceScene& S, const float4* rays, uint32_t 
                              unsigned long long* stats, cudaStream_t st) {
   constexpr int T = 128, M = 10, R = 16;  // the default ray-query shape
   const bool big = S.stack_need > 64u;
-  // node visits per iteration of the bounce queries (RT_TRACE_RAW_VISITS, 1 or 2)
-  // (config 2 extended: 3.44 against 3.51 ms per frame with two)
-  static const int visits = env_int("RT_TRACE_RAW_VISITS", 2) == 1 ? 1 : 2;
-  const int k = (big ? 1 : 0) | (stats ? 2 : 0) | (visits == 2 ? 4 : 0);
-  static int bps[8] = {-1, -1, -1, -1, -1, -1, -1, -1};
-  static const TraceKernel table[8] = {
+  // node visits per iteration of the bounce queries (RT_TRACE_RAW_VISITS, 1-4)
+  // (config 2 extended: 3.44 against 3.51 ms per frame with two than one)
+  static const int visits = std::min(4, std::max(1, env_int("RT_TRACE_RAW_VISITS", 2)));
+  const int k = (big ? 1 : 0) | (stats ? 2 : 0) | ((visits - 1) << 2);
+  static int bps[16] = {-1, -1, -1, -1, -1, -1, -1, -1, -1, -1, -1, -1, -1, -1, -1, -1};
+  static const TraceKernel table[16] = {
       k_trace_step<false, 64, T, M, false, true, R>,         k_trace_step<false, 192, T, M, false, true, R>,
       k_trace_step<false, 64, T, M, true, true, R>,          k_trace_step<false, 192, T, M, true, true, R>,
       k_trace_step<false, 64, T, M, false, true, R, false, 0, 2>, k_trace_step<false, 192, T, M, false, true, R, false, 0, 2>,
-      k_trace_step<false, 64, T, M, true, true, R, false, 0, 2>,  k_trace_step<false, 192, T, M, true, true, R, false, 0, 2>};
+      k_trace_step<false, 64, T, M, true, true, R, false, 0, 2>,  k_trace_step<false, 192, T, M, true, true, R, false, 0, 2>,
+      k_trace_step<false, 64, T, M, false, true, R, false, 0, 3>, k_trace_step<false, 192, T, M, false, true, R, false, 0, 3>,
+      k_trace_step<false, 64, T, M, true, true, R, false, 0, 3>,  k_trace_step<false, 192, T, M, true, true, R, false, 0, 3>,
+      k_trace_step<false, 64, T, M, false, true, R, false, 0, 4>, k_trace_step<false, 192, T, M, false, true, R, false, 0, 4>,
+      k_trace_step<false, 64, T, M, true, true, R, false, 0, 4>,  k_trace_step<false, 192, T, M, true, true, R, false, 0, 4>};
   TraceKernel kern = table[k];
   int per_sm = 0;
   if (cudaError_t e = cached_blocks_per_sm(&bps[k], kern, T, &per_sm); e != cudaSuccess) return e;
