@@ -48,7 +48,7 @@ SEED = 3
 CPU_SAMPLE = 2_097_152
 # DRAM bytes per ray of k_trace_step on the full config-3 BVH: one ncu capture
 # of a 2,097,152-ray launch, dram__bytes_read.sum + dram__bytes_write.sum.
-DRAM_BYTES_PER_RAY = (1.402943e9 + 60.078848e6) / 2_097_152  # ncu, 2 Mi-ray launch on the config-3 tree
+DRAM_BYTES_PER_RAY = (1.334632e9 + 59.1296e6) / 2_097_152  # ncu, 2 Mi-ray launch on the config-3 tree
 
 
 def parse():

@@ -253,7 +253,10 @@ enum {
                             its t and edge decisions round differently. */
 };
 
-/* Traces n rays resident on the device; writes n hits.  Stream-ordered. */
+/* Traces n rays resident on the device; writes n hits.  Stream-ordered.
+ * d_rays must be 16-byte aligned and d_hits 8-byte aligned (RT_EINVAL
+ * otherwise), as any cudaMalloc'd RtRay / RtHit array or slice of one is;
+ * the same holds for every entry point that takes device rays and hits. */
 rt_status rt_trace(rt_scene* scene, const RtRay* d_rays, uint32_t n, RtHit* d_hits,
                    uint32_t flags, void* stream);
 /* Same with host buffers (pinned or pageable): the library stages the rays

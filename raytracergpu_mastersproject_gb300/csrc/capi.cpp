@@ -487,11 +487,20 @@ rt_status rt_scene_get_nodes(const rt_scene* scene, RtBVHNode40* h_out, uint32_t
   return RT_OK;
 }
 
+// Device ray and hit arrays must sit at their records' natural vector
+// alignment: the kernels read a ray as float4 pairs (16 bytes) and write a hit
+// as one 8-byte store.  Any cudaMalloc'd array of RtRay / RtHit, or a slice of
+// one, satisfies it; a byte offset that breaks it is refused rather than
+// faulting on the device.
+static bool misaligned(const void* rays, const void* hits) {
+  return (reinterpret_cast<uintptr_t>(rays) & 15u) != 0u || (reinterpret_cast<uintptr_t>(hits) & 7u) != 0u;
+}
+
 rt_status rt_trace(rt_scene* scene, const RtRay* d_rays, uint32_t n, RtHit* d_hits, uint32_t flags, void* stream) {
   rtgb::NvtxRange nvtx_range("rt_trace");
   if (!scene || (n && (!d_rays || !d_hits)) || flags > (RT_TRACE_ANY | RT_TRACE_SORT | RT_TRACE_MT) ||
-      n > 0x80000000u) {
-    set_error("rt_trace: bad argument");
+      n > 0x80000000u || misaligned(d_rays, d_hits)) {
+    set_error("rt_trace: bad argument (rays must be 16-byte aligned, hits 8-byte aligned)");
     return RT_EINVAL;
   }
   if (n == 0) return RT_OK;
@@ -513,8 +522,8 @@ rt_status rt_trace_count(rt_scene* scene, const RtRay* d_rays, uint32_t n, RtHit
                          void* stream, uint64_t* h_counts) {
   rtgb::NvtxRange nvtx_range("rt_trace_count");
   if (!scene || !h_counts || (n && (!d_rays || !d_hits)) || flags > (RT_TRACE_ANY | RT_TRACE_SORT) ||
-      n > 0x80000000u) {
-    set_error("rt_trace_count: bad argument");
+      n > 0x80000000u || misaligned(d_rays, d_hits)) {
+    set_error("rt_trace_count: bad argument (rays must be 16-byte aligned, hits 8-byte aligned)");
     return RT_EINVAL;
   }
   h_counts[0] = h_counts[1] = 0;
@@ -542,8 +551,10 @@ rt_status rt_trace_count(rt_scene* scene, const RtRay* d_rays, uint32_t n, RtHit
 rt_status rt_trace_autotune(rt_scene* scene, const RtRay* d_rays, uint32_t n, RtHit* d_hits, uint32_t flags,
                             void* stream, uint32_t repeats, RtTraceTuning* out) {
   rtgb::NvtxRange nvtx_range("rt_trace_autotune");
-  if (!scene || !d_rays || !d_hits || n == 0 || n > 0x80000000u || (flags & ~(uint32_t)(RT_TRACE_ANY | RT_TRACE_SORT))) {
-    set_error("rt_trace_autotune: bad argument (rays and hits required; flags RT_TRACE_ANY / RT_TRACE_SORT)");
+  if (!scene || !d_rays || !d_hits || n == 0 || n > 0x80000000u || (flags & ~(uint32_t)(RT_TRACE_ANY | RT_TRACE_SORT)) ||
+      misaligned(d_rays, d_hits)) {
+    set_error("rt_trace_autotune: bad argument (rays and hits required, 16- and 8-byte aligned; flags RT_TRACE_ANY / "
+              "RT_TRACE_SORT)");
     return RT_EINVAL;
   }
   if (repeats == 0) repeats = 3;
@@ -701,7 +712,8 @@ rt_status rt_trace_host(rt_scene* scene, const RtRay* h_rays, uint32_t n, RtHit*
   }();
   if (kDirectHits) {
     cudaPointerAttributes pa;
-    if (cudaPointerGetAttributes(&pa, h_hits) == cudaSuccess && pa.type == cudaMemoryTypeHost && pa.devicePointer)
+    if (cudaPointerGetAttributes(&pa, h_hits) == cudaSuccess && pa.type == cudaMemoryTypeHost && pa.devicePointer &&
+        !misaligned(nullptr, pa.devicePointer))
       direct = static_cast<RtHit*>(pa.devicePointer);
     else
       cudaGetLastError();  // an unregistered pointer is not an error here

@@ -152,7 +152,9 @@ __global__ void __launch_bounds__(THREADS, MINB)
           local = g - __ldg(&jobs[job].start);
           const float4* rays = jobs[job].rays;
           const uint32_t root = __ldg(&jobs[job].root);
-          dev::trav_init_ray(s, __ldg(&rays[2u * local]), __ldg(&rays[2u * local + 1u]), root);
+          float4 ro, rd;
+          dev::load_ray(rays, local, dev::aligned32(rays), ro, rd);
+          dev::trav_init_ray(s, ro, rd, root);
           if constexpr (TILE > 0) {
             fetch.tile = tile_base + 4u * TILE * job;
             fetch.base = root;
@@ -193,7 +195,7 @@ __global__ void __launch_bounds__(THREADS, MINB)
         h.x = __ldg(&S.tri_ids[s.best & kSlotMask]);
         h.y = __float_as_uint(s.tclose);
       }
-      jobs[job].hits[local] = h;
+      __stcs(&jobs[job].hits[local], h);  // written once: evict-first
       local = 0xFFFFFFFFu;
     }
   }
@@ -446,6 +448,10 @@ rt_status fill_table(rt_pool* P, const RtJob* jobs, uint32_t num_jobs, DJob* hos
     }
     if (J.num_rays && (!J.d_rays || !J.d_hits)) {
       set_error("rt_pool_trace: job " + std::to_string(j) + " has null ray/hit buffers");
+      return RT_EINVAL;
+    }
+    if ((reinterpret_cast<uintptr_t>(J.d_rays) & 15u) != 0u || (reinterpret_cast<uintptr_t>(J.d_hits) & 7u) != 0u) {
+      set_error("rt_pool_trace: job " + std::to_string(j) + ": rays must be 16-byte aligned, hits 8-byte aligned");
       return RT_EINVAL;
     }
     out[j].rays = reinterpret_cast<const float4*>(J.d_rays);

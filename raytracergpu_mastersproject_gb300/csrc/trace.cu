@@ -42,6 +42,7 @@ __global__ void __launch_bounds__(THREADS, MINB)
   uint32_t ray = 0xFFFFFFFFu;
   bool exhausted = false;
   unsigned long long vis = 0, tests = 0;
+  const bool rays_al32 = dev::aligned32(rays);
   for (;;) {
     const bool idle = ray == 0xFFFFFFFFu;
     const uint32_t m = __ballot_sync(0xFFFFFFFFu, idle);
@@ -57,7 +58,9 @@ __global__ void __launch_bounds__(THREADS, MINB)
           if (dev::chk(S.check, ray >= n, dev::kChkRay, ray)) {
             ray = 0xFFFFFFFFu;
           } else {
-            dev::trav_init_ray(s, __ldg(&rays[2u * ray]), __ldg(&rays[2u * ray + 1u]), S.root);
+            float4 ro, rd;
+            dev::load_ray(rays, ray, rays_al32, ro, rd);
+            dev::trav_init_ray(s, ro, rd, S.root);
             if constexpr (W == 2) stack[0] = kSentinel;
           }
         }
@@ -82,7 +85,7 @@ __global__ void __launch_bounds__(THREADS, MINB)
           h.x = __ldg(&S.tri_ids[s.best & kSlotMask]);
           h.y = __float_as_uint(s.tclose);
         }
-        hits[ray] = h;
+        __stcs(&hits[ray], h);
         if constexpr (STATS) {
           vis += s.nvis;
           tests += s.ntest;
@@ -163,6 +166,7 @@ __global__ void __launch_bounds__(THREADS, MINB)
   bool exhausted = false;
   unsigned long long vis = 0, tests = 0;
   const int min_idle = refill < 1 ? 1 : (refill > 32 ? 32 : refill);
+  const bool rays_al32 = dev::aligned32(rays);
   for (;;) {
     const uint32_t idle = __ballot_sync(0xFFFFFFFFu, ray == 0xFFFFFFFFu);
     if (exhausted && idle == 0xFFFFFFFFu) break;
@@ -175,7 +179,9 @@ __global__ void __launch_bounds__(THREADS, MINB)
         const uint32_t id = base + (uint32_t)__popc(idle & lanemask_lt());
         if (id < n && !dev::chk(S.check, order && __ldg(&order[id]) >= n, dev::kChkRay, order ? __ldg(&order[id]) : id)) {
           ray = order ? __ldg(&order[id]) : id;
-          dev::trav_init_ray(s, __ldg(&rays[2u * ray]), __ldg(&rays[2u * ray + 1u]), S.root);
+          float4 ro, rd;
+          dev::load_ray(rays, ray, rays_al32, ro, rd);
+          dev::trav_init_ray(s, ro, rd, S.root);
           stk.reset();
           if (s.leaf != 0u) {  // the whole tree is one leaf
             s.node = s.leaf;
@@ -218,7 +224,10 @@ __global__ void __launch_bounds__(THREADS, MINB)
         h.x = __ldg(&S.tri_ids[s.best & kSlotMask]);
         h.y = __float_as_uint(s.tclose);
       }
-      hits[ray] = h;
+      if (RAW)
+        hits[ray] = h;  // read back by the shading kernel next
+      else
+        __stcs(&hits[ray], h);  // written once: evict-first
       if constexpr (STATS) {
         vis += s.nvis;
         tests += s.ntest;
@@ -484,8 +493,9 @@ extern "C" rt_status rt_trace_noalloc(rt_scene* scene, const RtRay* d_rays, uint
                                       uint32_t flags, void* stream) {
   rtgb::NvtxRange nvtx_range("rt_trace_noalloc");
   using namespace rtgb;
-  if (!scene || (n && (!d_rays || !d_hits)) || (flags & ~(uint32_t)(RT_TRACE_ANY | RT_TRACE_MT))) {
-    set_error("rt_trace_noalloc: bad argument");
+  if (!scene || (n && (!d_rays || !d_hits)) || (flags & ~(uint32_t)(RT_TRACE_ANY | RT_TRACE_MT)) ||
+      (reinterpret_cast<uintptr_t>(d_rays) & 15u) != 0u || (reinterpret_cast<uintptr_t>(d_hits) & 7u) != 0u) {
+    set_error("rt_trace_noalloc: bad argument (rays must be 16-byte aligned, hits 8-byte aligned)");
     return RT_EINVAL;
   }
   if (n > RT_NOALLOC_MAX_RAYS) {

@@ -23,20 +23,51 @@ __device__ __forceinline__ float4 ldg4(const void* base, uint32_t idx) {
   return __ldg(reinterpret_cast<const float4*>(base) + idx);
 }
 __device__ __forceinline__ uint32_t fbits(float f) { return __float_as_uint(f); }
+// Two consecutive float4 (32 bytes, 32-byte aligned) in one 256-bit load
+// through the read-only path (sm_100 and later): a node or triangle record
+// takes two loads instead of four, each one whole 32-byte sector (config 3:
+// 11.28 -> 10.2 ms per step).  idx2 counts 32-byte units.
+__device__ __forceinline__ void ldg8(const void* base, uint32_t idx2, float4& a, float4& b) {
+  const float4* p = reinterpret_cast<const float4*>(base) + 2u * idx2;
+  asm("ld.global.nc.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+      : "=f"(a.x), "=f"(a.y), "=f"(a.z), "=f"(a.w), "=f"(b.x), "=f"(b.y), "=f"(b.z), "=f"(b.w)
+      : "l"(p));
+}
+// The same for tree nodes, marked to stay in L2 ahead of streamed data
+// (rays, hits), which is marked evict-first.
+__device__ __forceinline__ void ldg8_keep(const void* base, uint32_t idx2, float4& a, float4& b) {
+  const float4* p = reinterpret_cast<const float4*>(base) + 2u * idx2;
+  asm("ld.global.nc.L2::evict_last.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+      : "=f"(a.x), "=f"(a.y), "=f"(a.z), "=f"(a.w), "=f"(b.x), "=f"(b.y), "=f"(b.z), "=f"(b.w)
+      : "l"(p));
+}
+// One 32-byte ray record (origin, tmin | direction, tmax), read once: a
+// single 256-bit load that skips L1 and leaves L2 first when the caller's
+// array is 32-byte aligned (`al32`, uniform per launch), else two loads.
+__device__ __forceinline__ void load_ray(const float4* rays, uint32_t i, bool al32, float4& o, float4& d) {
+  if (al32) {
+    asm("ld.global.nc.L1::no_allocate.L2::evict_first.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+        : "=f"(o.x), "=f"(o.y), "=f"(o.z), "=f"(o.w), "=f"(d.x), "=f"(d.y), "=f"(d.z), "=f"(d.w)
+        : "l"(rays + 2u * i));
+  } else {
+    o = __ldg(&rays[2u * i]);
+    d = __ldg(&rays[2u * i + 1u]);
+  }
+}
+__device__ __forceinline__ bool aligned32(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 31u) == 0u; }
 
 // ------------------------------------------------------- triangle test ----
 // triangleHit (raytraceBVH.comp:118-149) on a precomputed 64-byte record;
 // returns true and t for a hit in [tmin, tmax].  A NaN t never hits.
 __device__ __forceinline__ bool tri_test(const void* tris, uint32_t slot, float ox, float oy, float oz,
                                          float dx, float dy, float dz, float tmin, float tmax, float& t_out) {
-  const float4 r0 = ldg4(tris, 4u * slot + 0u);  // n.xyz, D
+  float4 r0, r1, r2, r3;
+  ldg8(tris, 2u * slot + 0u, r0, r1);  // n.xyz, D | w.xyz, v0.x
   const float denom = r0.x * dx + r0.y * dy + r0.z * dz;
   if (fabsf(denom) < 0.0001f) return false;
   const float t = (r0.w - (r0.x * ox + r0.y * oy + r0.z * oz)) / denom;
   if (!(t >= tmin && t <= tmax)) return false;  // a NaN t misses
-  const float4 r1 = ldg4(tris, 4u * slot + 1u);  // w.xyz, v0.x
-  const float4 r2 = ldg4(tris, 4u * slot + 2u);  // v0.y, v0.z, u.x, u.y
-  const float4 r3 = ldg4(tris, 4u * slot + 3u);  // u.z, v.x, v.y, v.z
+  ldg8(tris, 2u * slot + 1u, r2, r3);  // v0.y, v0.z, u.x, u.y | u.z, v.x, v.y, v.z
   const float px = ox + t * dx, py = oy + t * dy, pz = oz + t * dz;
   const float qx = px - r1.w, qy = py - r2.x, qz = pz - r2.y;
   const float ux = r2.z, uy = r2.w, uz = r3.x;
@@ -59,9 +90,10 @@ __device__ __forceinline__ bool tri_test(const void* tris, uint32_t slot, float 
 // (RT_TRACE_MT), not the reference's test.
 __device__ __forceinline__ bool tri_test_mt(const void* tris, uint32_t slot, float ox, float oy, float oz,
                                             float dx, float dy, float dz, float tmin, float tmax, float& t_out) {
-  const float4 r1 = ldg4(tris, 4u * slot + 1u);  // w.xyz, v0.x
-  const float4 r2 = ldg4(tris, 4u * slot + 2u);  // v0.y, v0.z, e1.x, e1.y
-  const float4 r3 = ldg4(tris, 4u * slot + 3u);  // e1.z, e2.x, e2.y, e2.z
+  float4 r0, r1, r2, r3;
+  ldg8(tris, 2u * slot + 0u, r0, r1);  // (n, D: unused) | w.xyz, v0.x
+  ldg8(tris, 2u * slot + 1u, r2, r3);  // v0.y, v0.z, e1.x, e1.y | e1.z, e2.x, e2.y, e2.z
+  (void)r0;
   const float e1x = r2.z, e1y = r2.w, e1z = r3.x;
   const float e2x = r3.y, e2y = r3.z, e2z = r3.w;
   const float px = dy * e2z - dz * e2y, py = dz * e2x - dx * e2z, pz = dx * e2y - dy * e2x;
@@ -252,10 +284,9 @@ __device__ __forceinline__ bool trav_run(const DeviceScene& S, Trav& s, uint32_t
         return false;
       }
       s.nvis++;
-      const float4 a = ldg4(S.inner, 4u * s.node + 0u);
-      const float4 b = ldg4(S.inner, 4u * s.node + 1u);
-      const float4 c = ldg4(S.inner, 4u * s.node + 2u);
-      const float4 d = ldg4(S.inner, 4u * s.node + 3u);
+      float4 a, b, c, d;
+      ldg8_keep(S.inner, 2u * s.node + 0u, a, b);
+      ldg8_keep(S.inner, 2u * s.node + 1u, c, d);
       float n0, f0, n1, f1;
       slab(s, a.x, a.y, a.z, a.w, c.x, c.y, n0, f0);
       slab(s, b.x, b.y, b.z, b.w, c.z, c.w, n1, f1);
@@ -427,10 +458,8 @@ __device__ __forceinline__ float qbyte(uint32_t w) {
 struct GlobalNodes {
   __device__ __forceinline__ void operator()(const DeviceScene& S, uint32_t node, float4& h, float4& r, float4& qa,
                                              float4& qb) const {
-    h = ldg4(S.inner, 4u * node + 0u);
-    r = ldg4(S.inner, 4u * node + 1u);
-    qa = ldg4(S.inner, 4u * node + 2u);
-    qb = ldg4(S.inner, 4u * node + 3u);
+    ldg8_keep(S.inner, 2u * node + 0u, h, r);
+    ldg8_keep(S.inner, 2u * node + 1u, qa, qb);
   }
 };
 // ... or, for the K nodes [base, base + K) -- the top levels of a tree, which

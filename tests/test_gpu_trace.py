@@ -572,3 +572,33 @@ def test_autotune_and_every_tuning_same_hits(rt, orc, cuda):
             sc.set_tuning(rt.TraceTuning(3, 5, 64, 16, 0.0))  # tiles only on the default shape
     ref, _ = orc.trace(orc.Scene(tris, orc.build_bvh(tris, mode=0)[0]), rays[:50_000], canonical=True)
     assert_parity(orc, tris, rays[:50_000], ref, base[:50_000])
+
+
+def test_ray_and_hit_alignment(rt, orc, cuda):
+    """Rays are read as one 32-byte load when the array is 32-byte aligned and
+    as two 16-byte loads otherwise, with the same hits; a ray array off a
+    16-byte boundary or a hit array off an 8-byte boundary is refused with
+    RT_EINVAL before anything is launched."""
+    tris = rt.gen_soup(5, 0, 20_000, 1.0, 0.01)
+    rays = rt.gen_rays(5, 0, 30_000, 1.0, 1e-4, float("inf"))
+    n = len(rays)
+    f = rt.lib().rt_trace
+    with rt.Scene(tris) as sc:
+        ref = dev_trace(rt, cuda, sc, rays)
+        raw = cuda.from_numpy(rays.view(np.uint8)).cuda()
+        buf = cuda.zeros(n * 32 + 64, dtype=cuda.uint8, device="cuda")
+        hits = cuda.full((n * 8 + 64,), 0xAB, dtype=cuda.uint8, device="cuda")
+        assert buf.data_ptr() % 256 == 0 and hits.data_ptr() % 256 == 0
+        st = cuda.cuda.current_stream().cuda_stream
+        for flags in (0, 2):  # as given, and origin-bucketed
+            for off in (16, 32, 48):  # 16-byte aligned, not always 32
+                buf[off:off + n * 32].copy_(raw)
+                hits.fill_(0xAB)
+                assert f(sc.handle, buf.data_ptr() + off, n, hits.data_ptr() + 8, flags, st) == 0
+                cuda.cuda.synchronize()
+                got = hits[8:8 + n * 8].cpu().numpy().view(rt.HIT_DTYPE)
+                assert np.array_equal(got.view(np.uint64), ref.view(np.uint64)), (flags, off)
+        for roff, hoff in ((4, 0), (8, 0), (0, 4)):
+            assert f(sc.handle, buf.data_ptr() + roff, n, hits.data_ptr() + hoff, 0, st) == 1  # RT_EINVAL
+            assert b"aligned" in rt.lib().rt_last_error_string()
+    assert (ref["prim"] != orc.NO_HIT).sum() > n // 10
