@@ -49,6 +49,11 @@ CPU_SAMPLE = 2_097_152
 # DRAM bytes per ray of k_trace_step on the full config-3 BVH: one ncu capture
 # of a 2,097,152-ray launch, dram__bytes_read.sum + dram__bytes_write.sum.
 DRAM_BYTES_PER_RAY = (1.334632e9 + 59.1296e6) / 2_097_152  # ncu, 2 Mi-ray launch on the config-3 tree
+# The same capture: L2 -> L1 bytes per ray (missed global-load sectors x 32 B)
+# and the FP32 (FMA) and ALU pipe activity of the kernel.
+L2_TO_L1_BYTES_PER_RAY = 182_466_249 * 32 / 2_097_152
+FMA_PIPE_PCT, ALU_PIPE_PCT = 29.6, 66.8
+NOMINAL_HBM_GBS = 8000.0  # GB300 HBM3e, nominal
 
 
 def parse():
@@ -665,7 +670,13 @@ def run_ours(args):
                           + ("; the step also runs the 3 reorder kernels" if sort else ""),
                 "gpu_node_fetches_per_ray": gpu_nodes / n, "gpu_prim_tests_per_ray": gpu_tests / n,
                 "fetched_bytes_per_ray": 40 + 64 * gpu_nodes / n + 64 * gpu_tests / n,
-                "avg_launch_ms": avg_launch * 1e3}
+                "avg_launch_ms": avg_launch * 1e3,
+                "frac_of_nominal_8TBps": achieved / NOMINAL_HBM_GBS}
+        if full3:
+            roof["ncu_2Mi_ray_launch"] = {"l2_to_l1_bytes_per_ray": L2_TO_L1_BYTES_PER_RAY,
+                                          "dram_bytes_per_ray": DRAM_BYTES_PER_RAY,
+                                          "fp32_fma_pipe_active_pct": FMA_PIPE_PCT,
+                                          "alu_pipe_active_pct": ALU_PIPE_PCT}
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",

@@ -596,7 +596,7 @@ rt_status rt_trace_autotune(rt_scene* scene, const RtRay* d_rays, uint32_t n, Rt
   };
   // 1. launch shape x refill threshold; 2. at the default shape, the stack
   // capacity and the top-of-tree staging tile.
-  static const int shapes[] = {kTunedVariant, 13, 10, 11, 8, 9, 6, 7, 3, 4};
+  static const int shapes[] = {kTunedVariant, 13, 14, 15, 10, 11, 8, 9, 6, 7, 3, 4};
   static const int refills[] = {3, 5, 8};
   TraceTuning t = default_tuning();
   t.stack = 0;

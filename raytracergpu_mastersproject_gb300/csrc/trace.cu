@@ -303,15 +303,18 @@ Variant make_variant() {
 // loop with the stack in local memory, 6 step loop at 10 blocks of 128
 // threads with a 16-entry shared ring, 7 the same as 5 blocks of 256; 8-9,
 // 10-11 and 12-13 are the shapes of 6 and 7 with up to two, three and four
-// node visits per iteration.  12 is the default (config 3: 11.78 ms per step
-// against 13.24 with one visit; six and eight visits were slower again).
+// node visits per iteration; 14-15 the four-visit shapes with the whole
+// stack in local memory (no ring: all of L1 stays cache).  12 is the default
+// (config 3: 11.78 ms per step against 13.24 with one visit; six and eight
+// visits were slower again).
 // Binary trees always use the while-while loop of the chosen shape.
 Variant g_variants[] = {make_variant<128, 12, false>(), make_variant<128, 10, false>(), make_variant<128, 1, false>(),
                         make_variant<128, 12, true>(),  make_variant<128, 10, true>(),  make_variant<128, 1, true>(),
                         make_variant<128, 10, true, 16>(), make_variant<256, 5, true, 16>(),
                         make_variant<128, 10, true, 16, 2>(), make_variant<256, 5, true, 16, 2>(),
                         make_variant<128, 10, true, 16, 3>(), make_variant<256, 5, true, 16, 3>(),
-                        make_variant<128, 10, true, 16, 4>(), make_variant<256, 5, true, 16, 4>()};
+                        make_variant<128, 10, true, 16, 4>(), make_variant<256, 5, true, 16, 4>(),
+                        make_variant<128, 10, true, 0, 4>(), make_variant<256, 5, true, 0, 4>()};
 constexpr int kNumVariants = sizeof(g_variants) / sizeof(g_variants[0]);
 
 // RT_TRACE_MT: the Moller-Trumbore leaf test in the default launch shape (the

@@ -566,6 +566,18 @@ def test_autotune_and_every_tuning_same_hits(rt, orc, cuda):
                                       base_any.view(np.uint64)), (stack, tile)
         host = sc.trace_host(rays)
         assert np.array_equal(host.view(np.uint64), base.view(np.uint64))
+        shapes = 0
+        while True:  # every launch shape the library has, until the first unknown one
+            try:
+                sc.set_tuning(rt.TraceTuning(shapes, 5, 0, 0, 0.0))
+            except rt.RtError:
+                break
+            assert np.array_equal(dev_trace(rt, cuda, sc, rays, sort=True).view(np.uint64),
+                                  base.view(np.uint64)), shapes
+            assert np.array_equal(dev_trace(rt, cuda, sc, rays, any_hit=True).view(np.uint64),
+                                  base_any.view(np.uint64)), shapes
+            shapes += 1
+        assert shapes >= 16
         with pytest.raises(rt.RtError):
             sc.set_tuning(rt.TraceTuning(12, 5, 8, 0, 0.0))    # below the tree's worst case
         with pytest.raises(rt.RtError):
