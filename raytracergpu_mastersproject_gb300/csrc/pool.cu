@@ -98,12 +98,12 @@ struct PoolTiledNodes {
 template <bool ANY, int STACK, int THREADS, int MINB, int RING, int TILE = 0, int VISITS = 1>
 __global__ void __launch_bounds__(THREADS, MINB)
     k_pool_step(DeviceScene S, const DJob* __restrict__ table, uint32_t* __restrict__ counter, int refill) {
-  uint2 stack[STACK];
-  using Stk = typename std::conditional<(RING > 0), dev::RingStack<(RING > 0 ? RING : 1), THREADS>,
-                                        dev::LocalStack>::type;
+  dev::StepEntry stack[STACK];
+  using Stk = typename std::conditional<(RING > 0), dev::RingStack<(RING > 0 ? RING : 1), THREADS, dev::StepEntry>,
+                                        dev::LocalStackT<dev::StepEntry>>::type;
   Stk stk;
   if constexpr (RING > 0) {
-    __shared__ uint2 ring[RING * THREADS];
+    __shared__ dev::StepEntry ring[RING * THREADS];
     stk.ring = ring + threadIdx.x;
     stk.spill = stack;
     stk.lo = 0;

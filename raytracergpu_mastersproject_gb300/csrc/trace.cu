@@ -120,7 +120,7 @@ __global__ void __launch_bounds__(THREADS, MINB)
 // none, kRawOverflow: stack overflow) and t -- so that shading needs no id map.
 //
 // RING > 0 keeps the top RING stack entries of each lane in shared memory
-// (RING * THREADS * 8 bytes per block), the rest in local memory.
+// (RING * THREADS * 4 bytes per block: refs only), the rest in local memory.
 //
 // TILE > 0 stages the tree's first TILE nodes -- its top levels, numbered
 // first in breadth-first order -- in shared memory per block (plain loads at
@@ -136,12 +136,12 @@ __global__ void __launch_bounds__(THREADS, MINB)
     k_trace_step(DeviceScene S, const float4* __restrict__ rays, uint32_t n, uint2* __restrict__ hits,
                  uint32_t* __restrict__ counter, int refill, unsigned long long* __restrict__ stats,
             const uint32_t* __restrict__ order) {
-  uint2 stack[STACK];
-  using Stk = typename std::conditional<(RING > 0), dev::RingStack<(RING > 0 ? RING : 1), THREADS>,
-                                        dev::LocalStack>::type;
+  dev::StepEntry stack[STACK];
+  using Stk = typename std::conditional<(RING > 0), dev::RingStack<(RING > 0 ? RING : 1), THREADS, dev::StepEntry>,
+                                        dev::LocalStackT<dev::StepEntry>>::type;
   Stk stk;
   if constexpr (RING > 0) {
-    __shared__ uint2 ring[RING * THREADS];
+    __shared__ dev::StepEntry ring[RING * THREADS];
     stk.ring = ring + threadIdx.x;
     stk.spill = stack;
     stk.lo = 0;
@@ -251,7 +251,8 @@ using TraceKernel = void (*)(DeviceScene, const float4*, uint32_t, uint2*, uint3
                              const uint32_t*);
 
 // Stack capacities: binary trees 64 or 128 refs (depth + sentinel); 4-wide
-// trees 64 or 192 (ref, t) entries (worst-case pushes along a path).
+// trees 64 or 192 entries (worst-case pushes along a path; (ref, t_near) in
+// the while-while loop, the ref alone in the step loop).
 struct Variant {
   int threads, minb;
   TraceKernel k[2][2][2][2];  // [stats][wide][any][big stack]
