@@ -141,14 +141,29 @@ __global__ void __launch_bounds__(THREADS, MINB)
     const uint32_t idle = __ballot_sync(0xFFFFFFFFu, local == 0xFFFFFFFFu);
     if (exhausted && idle == 0xFFFFFFFFu) break;
     if (!exhausted && __popc(idle) >= min_idle) {
-      uint32_t base = 0;
-      if (lane == 0) base = atomicAdd(counter, (uint32_t)__popc(idle));
+      // One binary search per refill, for the first ray handed out; the
+      // warp's other new rays follow it in the queue, so each lane walks on
+      // from that job (jobs hold thousands of rays: rarely a step, and
+      // never more than 8 before it searches for itself).
+      uint32_t base = 0, first_job = 0;
+      if (lane == 0) {
+        base = atomicAdd(counter, (uint32_t)__popc(idle));
+        if (base < total) first_job = find_job(jobs, num_jobs, base);
+      }
       base = __shfl_sync(0xFFFFFFFFu, base, 0);
+      first_job = __shfl_sync(0xFFFFFFFFu, first_job, 0);
       if (base + (uint32_t)__popc(idle) >= total) exhausted = true;
       if (local == 0xFFFFFFFFu) {
         const uint32_t g = base + (uint32_t)__popc(idle & lanemask_lt_p());
         if (g < total) {
-          job = find_job(jobs, num_jobs, g);
+          job = first_job;
+          for (int k = 0; job + 1u < num_jobs && __ldg(&jobs[job + 1u].start) <= g; ++k) {
+            if (k == 8) {
+              job = find_job(jobs, num_jobs, g);
+              break;
+            }
+            ++job;
+          }
           local = g - __ldg(&jobs[job].start);
           const float4* rays = jobs[job].rays;
           const uint32_t root = __ldg(&jobs[job].root);
