@@ -48,11 +48,11 @@ SEED = 3
 CPU_SAMPLE = 2_097_152
 # DRAM bytes per ray of k_trace_step on the full config-3 BVH: one ncu capture
 # of a 2,097,152-ray launch, dram__bytes_read.sum + dram__bytes_write.sum.
-DRAM_BYTES_PER_RAY = (1.334632e9 + 59.1296e6) / 2_097_152  # ncu, 2 Mi-ray launch on the config-3 tree
+DRAM_BYTES_PER_RAY = (1.306393e9 + 58.430976e6) / 2_097_152  # ncu, 2 Mi-ray launch on the config-3 tree
 # The same capture: L2 -> L1 bytes per ray (missed global-load sectors x 32 B)
 # and the FP32 (FMA) and ALU pipe activity of the kernel.
-L2_TO_L1_BYTES_PER_RAY = 182_466_249 * 32 / 2_097_152
-FMA_PIPE_PCT, ALU_PIPE_PCT = 29.6, 66.8
+L2_TO_L1_BYTES_PER_RAY = 188_542_810 * 32 / 2_097_152
+FMA_PIPE_PCT, ALU_PIPE_PCT = 31.5, 67.1
 NOMINAL_HBM_GBS = 8000.0  # GB300 HBM3e, nominal
 
 

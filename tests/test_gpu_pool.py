@@ -94,6 +94,13 @@ def test_pool_budget_and_empty_jobs(rt, cuda):
         pool.trace([])
         with pytest.raises(rt.RtError):
             pool.trace([(999, d_rays, d_hits)])
+        # a job whose rays are off a 16-byte boundary, or hits off an 8-byte
+        # one, is refused before anything is launched
+        n = len(r) - 1
+        for rays_view, hits_view in ((d_rays[4:4 + n * 32], d_hits), (d_rays, d_hits[4:4 + n * 8])):
+            with pytest.raises(rt.RtError) as e:
+                pool.trace([(b, rays_view, hits_view, n)])
+            assert e.value.status == 1 and "aligned" in str(e.value)
 
 
 def test_pool_every_tuning_same_hits(rt, cuda):
