@@ -672,6 +672,13 @@ def run_ours(args):
                 "fetched_bytes_per_ray": 40 + 64 * gpu_nodes / n + 64 * gpu_tests / n,
                 "avg_launch_ms": avg_launch * 1e3,
                 "frac_of_nominal_8TBps": achieved / NOMINAL_HBM_GBS}
+        # the same launch measured in the bytes the kernel itself fetches (its
+        # own node and triangle fetches, GPU counters), and in DRAM bytes
+        fetched = roof["fetched_bytes_per_ray"] * n / avg_launch / 1e9
+        roof["fetched_GBps"], roof["fetched_frac"] = fetched, fetched / peak
+        if full3:
+            dram = DRAM_BYTES_PER_RAY * n / avg_launch / 1e9
+            roof["dram_GBps"], roof["dram_frac"] = dram, dram / peak
         if full3:
             roof["ncu_2Mi_ray_launch"] = {"l2_to_l1_bytes_per_ray": L2_TO_L1_BYTES_PER_RAY,
                                           "dram_bytes_per_ray": DRAM_BYTES_PER_RAY,
