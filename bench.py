@@ -628,7 +628,7 @@ def run_ours(args):
         barrier()
         e2e = {"value": n * ws / (dt / k) / 1e9, "unit": UNIT, "h2d_bytes_per_step": n * 32,
                "d2h_bytes_per_step": n * 8, "steps": k, "ms_per_step": dt / k * 1e3,
-               "path": "rt_trace_host, pinned host buffers: rays in chunks of 512 Ki, 2 Mi, 8 Mi, the rest but "
+               "path": "rt_trace_host, pinned host buffers: rays in chunks of 2 Mi, 8 Mi, the rest but "
                        "512 Ki, and 512 Ki, each uploaded on a copy stream while the one before traces (two trace "
                        "streams); hits staged in HBM and downloaded per chunk on a third stream"}
         hits_dev = d_hits.cpu().numpy().view(rt.HIT_DTYPE)

@@ -688,8 +688,8 @@ rt_status rt_trace_host(rt_scene* scene, const RtRay* h_rays, uint32_t n, RtHit*
   // (its upload is not overlapped) and each next one several times larger.
   //
   // Hits are staged in device memory and downloaded per chunk on a third
-  // stream; chunks grow 4x, and the plan ends with a small chunk, so that the
-  // one download that overlaps nothing is short.  With RT_HOST_DIRECT_HITS=1
+  // stream; chunks start at 2 Mi rays and grow 4x, and the plan ends with a
+  // small chunk, so that the one download that overlaps nothing is short.  With RT_HOST_DIRECT_HITS=1
   // and page-locked h_hits the kernels instead write the hits there directly
   // over the host link (scattered 8-byte stores, overlapped with tracing) and
   // chunks grow 8x; on GB300 that measured no faster than staging (config 3:
@@ -697,7 +697,7 @@ rt_status rt_trace_host(rt_scene* scene, const RtRay* h_rays, uint32_t n, RtHit*
   static const uint32_t kFirstChunk = [] {
     const char* e = std::getenv("RT_HOST_FIRST_CHUNK_RAYS");
     const long v = e ? std::atol(e) : 0;
-    return v >= 4096 && v <= (1l << 30) ? (uint32_t)v : (1u << 19);
+    return v >= 4096 && v <= (1l << 30) ? (uint32_t)v : (1u << 21);
   }();
   static const uint32_t kLastChunk = [] {
     const char* e = std::getenv("RT_HOST_LAST_CHUNK_RAYS");

@@ -123,11 +123,11 @@ def test_trace_host_matches_device(rt, cuda):
         b = sc.trace_host(rays)
         pinned = cuda.from_numpy(rays.view(np.uint8)).pin_memory()
         c = sc.trace_host(pinned.numpy().view(rt.RAY_DTYPE))
-        # 5 M rays: chunks of 512 Ki, 2 Mi and the rest, on both buffers and both trace streams
+        # 5 M rays: chunks of 2 Mi, the rest but 512 Ki, and 512 Ki, on both buffers and both trace streams
         d = sc.trace_host(pinned.numpy().view(rt.RAY_DTYPE), sort=True)
         e = sc.trace_host(pinned.numpy().view(rt.RAY_DTYPE), any_hit=True)
         f = dev_trace(rt, cuda, sc, rays, any_hit=True)
-        # page-locked hits: the kernels write them directly (chunks of 512 Ki, 4 Mi and the rest)
+        # page-locked hits: staged by default; with RT_HOST_DIRECT_HITS=1 the kernels write them directly
         out_t = cuda.full((len(rays) * 8,), 0xCD, dtype=cuda.uint8).pin_memory()
         out = out_t.numpy().view(rt.HIT_DTYPE)
         g = sc.trace_host(pinned.numpy().view(rt.RAY_DTYPE), out=out, sort=True).copy()
