@@ -684,16 +684,18 @@ rt_status rt_trace_host(rt_scene* scene, const RtRay* h_rays, uint32_t n, RtHit*
   // copy-in runs on a stream of its own, so chunk i+1 uploads while chunk i
   // traces, and chunk i+1's blocks take the SMs that chunk i's last rays
   // leave idle.  Every launch still ends with a drain of its in-flight rays at
-  // falling SIMT efficiency, so chunks are few and large: the first is small
-  // (its upload is not overlapped) and each next one several times larger.
+  // falling SIMT efficiency, so chunks are few and large: the first is the
+  // smallest (its upload is not overlapped) and each next one several times
+  // larger.
   //
   // Hits are staged in device memory and downloaded per chunk on a third
   // stream; chunks start at 2 Mi rays and grow 4x, and the plan ends with a
-  // small chunk, so that the one download that overlaps nothing is short.  With RT_HOST_DIRECT_HITS=1
-  // and page-locked h_hits the kernels instead write the hits there directly
-  // over the host link (scattered 8-byte stores, overlapped with tracing) and
-  // chunks grow 8x; on GB300 that measured no faster than staging (config 3:
-  // 12.55-13.03 ms against 12.36-12.55 ms per 16 Mi rays on the same boxes).
+  // small chunk, so that the one download that overlaps nothing is short.
+  // With RT_HOST_DIRECT_HITS=1 and page-locked h_hits the kernels instead
+  // write the hits there directly over the host link (scattered 8-byte
+  // stores, overlapped with tracing) and chunks grow 8x; on GB300 that
+  // measured no faster than staging (config 3: 12.55-13.03 ms against
+  // 12.36-12.55 ms per 16 Mi rays on the same boxes).
   static const uint32_t kFirstChunk = [] {
     const char* e = std::getenv("RT_HOST_FIRST_CHUNK_RAYS");
     const long v = e ? std::atol(e) : 0;
