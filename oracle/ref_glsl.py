@@ -9,7 +9,7 @@ built-ins) and oracle/ref_harness.cpp (dispatch entry points), into
 oracle/_ref/libref_glsl.so (sin/cos from libm) and
 oracle/_ref/libref_glsl_portable.so (the oracle's portable sin/cos).  The
 generated sources and libraries stay in oracle/_ref/, which is not committed.
-Without the reference checkout (the GPU host) previously generated sources in
+On a host without the reference checkout, previously generated sources in
 oracle/_ref/ are compiled again; with neither, nothing is built.
 
 The rewrite changes syntax only, never an expression:
