@@ -52,6 +52,32 @@ def test_pool_matches_individual_scenes(rt, cuda):
             assert np.array_equal(g.view(np.uint64), alone(rt, cuda, t, r).view(np.uint64))
 
 
+def test_pool_runs_of_empty_jobs(rt, cuda):
+    """Jobs with no rays between and around real ones: a refill's new rays
+    walk from the first ray's job over empty jobs, and past 8 of them search
+    the job table instead.  Every real job gets exactly its own hits."""
+    data = soups(rt, 44, 4, lo=5_000, hi=20_000)
+    with rt.Pool() as pool:
+        ids = [pool.add_scene(t) for t, _ in data]
+        zero = cuda.empty(8, dtype=cuda.uint8, device="cuda")
+        dr = [cuda.from_numpy(r.view(np.uint8)).cuda() for _, r in data]
+        dh = [cuda.full((len(r) * 8,), 0xEE, dtype=cuda.uint8, device="cuda") for _, r in data]
+        jobs = []
+        for k, (sid, a, b) in enumerate(zip(ids, dr, dh)):
+            jobs += [(sid, zero, zero, 0)] * (3 + 9 * k)  # 3, 12, 21, 30 empty jobs before each
+            jobs.append((sid, a, b))
+        jobs += [(ids[0], zero, zero, 0)] * 5
+        for variant in (5, 6):  # with and without the shared-memory ring
+            for h in dh:
+                h.fill_(0xEE)
+            pool.set_tuning(variant, 4)
+            pool.trace(jobs)
+            cuda.cuda.synchronize()
+            for (t, r), h in zip(data, dh):
+                got = h.cpu().numpy().view(rt.HIT_DTYPE)
+                assert np.array_equal(got.view(np.uint64), alone(rt, cuda, t, r).view(np.uint64)), variant
+
+
 def test_pool_remove_reuse_and_growth(rt, cuda):
     data = soups(rt, 42, 40, lo=20_000, hi=120_000)
     with rt.Pool() as pool:
