@@ -76,6 +76,7 @@ def parse():
     p.add_argument("--no-render", action="store_true", help="skip the config-2 path-tracing run")
     p.add_argument("--render-spp", type=int, default=16, help="samples per pixel of the config-2 frame")
     p.add_argument("--serve-requests", type=int, default=200)
+    p.add_argument("--serve-inflight", type=int, default=3, help="batches in flight at once (continuous batching)")
     p.add_argument("--serve-rates", type=str, default="250,500,1000,2000,4000,8000,16000",
                    help="Poisson arrival rates (requests/s), swept in order")
     return p.parse_args()
@@ -406,7 +407,7 @@ def serving_summary(runs: list[dict]) -> dict:
     return out
 
 
-def run_served(torch, rt, n_requests: int, rates: list[float]) -> dict:
+def run_served(torch, rt, n_requests: int, rates: list[float], inflight: int = 3) -> dict:
     """Config 5: 64 resident scenes, Poisson arrivals; 90% ray queries
     (log-uniform [1K, 2M] rays, closest-hit), 10% new-scene uploads; latency
     p50/p99 and rays/s with continuous batching vs plain sequential service."""
@@ -417,7 +418,7 @@ def run_served(torch, rt, n_requests: int, rates: list[float]) -> dict:
     resident = [wl.config5_scene(i) for i in range(n_scenes)]
     ray_pool_t = torch.from_numpy(rt.gen_rays(5, 0, 2_000_000, 1.0, 1e-4, float("inf")).view(np.uint8)).pin_memory()
     ray_pool = ray_pool_t.numpy().view(rt.RAY_DTYPE)
-    srv = rt.Server(budget_bytes=150 << 30, max_inflight=3, max_batch_rays=1 << 23)
+    srv = rt.Server(budget_bytes=150 << 30, max_inflight=inflight, max_batch_rays=1 << 23)
     sids = [srv.wait(srv.upload(t, build_on_device=True), 600.0).scene_id for t in resident]
     setup_s = time.perf_counter() - t0
     res_tris = int(sum(len(t) for t in resident))
@@ -432,7 +433,7 @@ def run_served(torch, rt, n_requests: int, rates: list[float]) -> dict:
                  "uploads": len(uploads), "rays": tot_rays}
         for mode in ("batched", "sequential"):
             if mode == "batched":
-                srv.set_batching(1024, 3)
+                srv.set_batching(1024, inflight)
             else:
                 srv.set_batching(1, 1)
             ids, kinds, new_scenes = [], [], []
@@ -652,7 +653,7 @@ def run_ours(args):
     batched = None if args.no_batched else run_batched(torch, rt)
     render = None if args.no_render else run_render(torch, rt, args.render_spp)
     served = None if args.no_served else run_served(
-        torch, rt, args.serve_requests, [float(x) for x in args.serve_rates.split(",") if x])
+        torch, rt, args.serve_requests, [float(x) for x in args.serve_rates.split(",") if x], args.serve_inflight)
     peak, peak_kind = measured_peak()
     cpu_base, counts, parity = None, None, None
     if not args.no_cpu:
